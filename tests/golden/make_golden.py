@@ -1,0 +1,116 @@
+"""
+Extract the dxtb test fixtures that pin the GFN-xTB path into ``golden.npz``.
+
+Run once in a checkout that has the dxtb source tree (read-only)::
+
+    python tests/golden/make_golden.py /path/to/dxtb
+
+Everything written here is copied verbatim from the dxtb test suite (fixture
+files and inline reference tensors, read as data); nothing is computed. The
+file records, per entry, which dxtb file it came from.
+"""
+
+from __future__ import annotations
+
+import ast
+import json
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).parent
+MOLS = ["H2", "LiH", "H2O", "CH4", "SiH4", "LYS_xao"]
+KEYS = {"H2": "h2", "LiH": "lih", "H2O": "h2o", "CH4": "ch4", "SiH4": "sih4", "LYS_xao": "lys_xao"}
+
+
+def _coord(path: Path, symbols: list[str]):
+    numbers, pos, active = [], [], False
+    for line in path.read_text().splitlines():
+        t = line.strip()
+        if t.startswith("$"):
+            active = t.startswith("$coord")
+            continue
+        if active and t:
+            f = t.split()
+            pos.append([float(v) for v in f[:3]])
+            numbers.append(symbols.index(f[3].lower()) + 1)
+    return np.array(numbers), np.array(pos)
+
+
+def _tensor_literals(src: str, func: str) -> dict[str, np.ndarray]:
+    """Literal ``torch.tensor([...])`` assignments inside one test function."""
+    tree = ast.parse(src)
+    out = {}
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == func:
+            for stmt in ast.walk(node):
+                if (
+                    isinstance(stmt, ast.Assign)
+                    and isinstance(stmt.targets[0], ast.Name)
+                    and isinstance(stmt.value, ast.Call)
+                    and getattr(stmt.value.func, "attr", "") == "tensor"
+                ):
+                    try:
+                        out[stmt.targets[0].id] = np.array(
+                            ast.literal_eval(stmt.value.args[0]), dtype=np.float64
+                        )
+                    except ValueError:
+                        pass
+    return out
+
+
+def _ref_vector(src: str) -> np.ndarray:
+    m = re.search(r"ref = torch.tensor\(\s*\[(.*?)\]", src, re.S)
+    return np.array(
+        [float(v) for v in re.findall(r"-?\d+\.\d+(?:[eE][-+]?\d+)?", m.group(1))]
+    )
+
+
+def main(ref_root: str) -> None:
+    root = Path(ref_root)
+    test = root / "test"
+    symbols = [
+        e["symbol"].lower()
+        for _, e in sorted(
+            json.load(open(HERE.parents[1] / "dxtb_gb300" / "data" / "gfn2.json"))[
+                "element"
+            ].items(),
+            key=lambda kv: int(kv[0]),
+        )
+    ]
+    g: dict[str, np.ndarray] = {}
+    src: dict[str, str] = {}
+    ov = np.load(test / "test_overlap" / "overlap.npz")
+    h0 = np.load(test / "test_hamiltonian" / "h0.npz")
+    gr = np.load(test / "test_scf" / "grad.npz")
+    for m in MOLS:
+        k = KEYS[m]
+        num, pos = _coord(test / "test_singlepoint" / "mols" / m / "coord", symbols)
+        g[f"{m}/numbers"] = num
+        g[f"{m}/positions"] = pos
+        g[f"{m}/overlap_gfn1"] = ov[k].astype(np.float64)
+        g[f"{m}/h0_gfn1"] = h0[k].astype(np.float64)
+        g[f"{m}/grad_elec_gfn1"] = gr[f"{k}_full"].astype(np.float64)
+    src["*/numbers,positions"] = "test/test_singlepoint/mols/*/coord"
+    src["*/overlap_gfn1"] = "test/test_overlap/overlap.npz (tblite 0.3.0)"
+    src["*/h0_gfn1"] = "test/test_hamiltonian/h0.npz (tblite 0.3.0)"
+    src["*/grad_elec_gfn1"] = (
+        "test/test_scf/grad.npz '<name>_full' (GFN1, rep/disp/hal excluded)"
+    )
+    for meth in ("gfn1", "gfn2"):
+        f = test / "test_scf" / f"test_elements_{meth}.py"
+        g[f"atoms/{meth}"] = _ref_vector(f.read_text())
+        src[f"atoms/{meth}"] = f"{f.relative_to(root)}: ref (tblite, E_scf - TS)"
+    aes = (test / "test_coulomb" / "test_aes2.py").read_text()
+    for func in ("test_energy", "test_potential"):
+        for name, arr in _tensor_literals(aes, func).items():
+            g[f"aes2_{func}/{name}"] = arr
+    src["aes2_*"] = "test/test_coulomb/test_aes2.py (LiH, inline tensors)"
+    np.savez_compressed(HERE / "golden.npz", **g)
+    (HERE / "golden_sources.json").write_text(json.dumps(src, indent=1))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
