@@ -1,0 +1,234 @@
+"""
+GFN1/GFN2-xTB calculators with the interface of dxtb's calculators.
+
+``GFN1Calculator(numbers, opts=..., device=..., dtype=...)`` and
+``GFN2Calculator`` expose ``get_energy``, ``get_forces``, ``singlepoint``,
+``energy``, ``forces`` and ``reset`` like the reference
+(calculators/gfn1.py, calculators/gfn2.py:267-298, calculators/types/
+abc.py:88-170, types/base.py:758-884). ``numbers`` is 1D for one molecule
+or 2D zero-padded for a batch (batch mode 1); positions are Bohr.
+
+Every number comes from the CUDA library (``libdxtb_gb300.so``): integrals,
+H0, interactions, the SCF and the analytic gradient. The energy is a
+``torch.autograd.Function`` whose backward multiplies the gradient from the
+adjoint kernels, so ``energy.backward()`` and ``torch.autograd.grad`` work on
+the positions as in the reference.
+
+Not computed (the reference's defaults include them): D3/D4 dispersion and
+the GFN1 halogen-bond term; callers wanting parity pass
+``opts={"exclude": ["disp", "hal"]}`` to the reference.
+"""
+
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+import torch
+
+from . import engine
+from .params import Tables
+
+__all__ = ["Calculator", "GFN1Calculator", "GFN2Calculator", "DtypeError", "DeviceError"]
+
+
+class DtypeError(ValueError):
+    """Mismatch of the floating-point type (types/base.py:833-864)."""
+
+
+class DeviceError(RuntimeError):
+    """Mismatch of the device (types/base.py:833-864)."""
+
+
+class SCFConvergenceError(RuntimeError):
+    """SCF did not converge and ``force_convergence`` was requested."""
+
+
+class SCFConvergenceWarning(UserWarning):
+    """SCF did not converge within ``maxiter``."""
+
+
+_TABLES: dict[str, Tables] = {}
+
+
+def tables(method: str) -> Tables:
+    if method not in _TABLES:
+        _TABLES[method] = Tables(method)
+    return _TABLES[method]
+
+
+class _Energy(torch.autograd.Function):
+    """Energy with the analytic gradient of the adjoint kernels as backward."""
+
+    @staticmethod
+    def forward(ctx, positions, calc, chrg, spin):
+        res = calc._run(positions.detach(), chrg, spin, forces=positions.requires_grad)
+        ctx.save_for_backward(res["gradient"] if res["gradient"] is not None else torch.empty(0))
+        ctx.shape = positions.shape
+        return res["energy"].to(positions.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        if g.numel() == 0:
+            return None, None, None, None
+        if grad_out.ndim == 0:
+            return grad_out * g, None, None, None
+        return grad_out.view(-1, *([1] * (g.ndim - 1))) * g, None, None, None
+
+
+class Calculator:
+    """GFN-xTB single-point calculator on one GB300."""
+
+    method = "gfn2"
+
+    def __init__(self, numbers, par=None, *, classical=None, interaction=None, opts=None,
+                 device=None, dtype=None, solvation: dict | None = None):
+        if par is not None and isinstance(par, str):
+            self.method = par
+        if not torch.is_tensor(numbers):
+            numbers = torch.as_tensor(numbers)
+        if numbers.dtype not in (torch.int16, torch.int32, torch.int64):
+            raise DtypeError(f"Atomic numbers must be integers, got {numbers.dtype}")
+        self.device = torch.device(device) if device is not None else numbers.device
+        if self.device.type != "cuda":
+            self.device = torch.device("cuda")
+        self.dtype = dtype or torch.float64
+        if self.dtype != torch.float64:
+            raise DtypeError("the GB300 path computes in float64 only")
+        self.numbers = numbers
+        self.batched = numbers.ndim > 1
+        self.opts = dict(opts or {})
+        self.solvation = solvation
+        if interaction is not None:
+            for it in interaction if isinstance(interaction, (list, tuple)) else [interaction]:
+                if isinstance(it, dict) and "epsilon" in it:
+                    self.solvation = it
+        excl = set(self.opts.get("exclude", []))
+        if not {"disp", "d4sc"}.issubset(excl) or (self.method == "gfn1" and "hal" not in excl):
+            warnings.warn(
+                "dispersion (and GFN1 halogen bonding) is not part of the GB300 path; "
+                "results equal the reference with exclude=['disp', 'd4sc', 'hal']",
+                stacklevel=2,
+            )
+        self.include_rep = "rep" not in excl
+        self.tables = tables(self.method)
+        nums = numbers.reshape(-1, numbers.shape[-1]).cpu().numpy()
+        self._mols = [n[n > 0] for n in nums]
+        for n in self._mols:
+            self.tables.check_elements(n)
+        self._pb: engine.PackedBatch | None = None
+        self._pb_key = None
+        self._state: dict = {}
+        self._cache: dict = {}
+
+    # ---- configuration (constants/defaults.py) ----
+    @property
+    def maxiter(self) -> int:
+        return int(self.opts.get("maxiter", 250))
+
+    @property
+    def etemp(self) -> float:
+        return float(self.opts.get("fermi_etemp", 300.0))
+
+    @property
+    def tol(self) -> float:
+        return float(self.opts.get("x_atol", self.opts.get("f_atol", 1e-10)))
+
+    def reset(self) -> None:
+        """Forget cached results (types/base.py:758-763)."""
+        self._cache.clear()
+
+    def _check(self, positions: torch.Tensor) -> None:
+        if positions.dtype != self.dtype:
+            raise DtypeError(f"positions have dtype {positions.dtype}, expected {self.dtype}")
+        if positions.device.type != "cuda":
+            raise DeviceError(f"positions on {positions.device}, expected a CUDA device")
+
+    def _chrg_list(self, chrg, nmol):
+        if torch.is_tensor(chrg):
+            c = chrg.detach().cpu().reshape(-1).tolist()
+        else:
+            c = np.atleast_1d(np.asarray(chrg, dtype=np.float64)).tolist()
+        return c * nmol if len(c) == 1 else c
+
+    def _run(self, positions, chrg=0.0, spin=None, forces=False):
+        self._check(positions)
+        pos = positions.reshape(-1, positions.shape[-2], 3)
+        nmol = len(self._mols)
+        chg = self._chrg_list(chrg, nmol)
+        spins = None if spin is None else self._chrg_list(spin, nmol)
+        key = (tuple(chg), None if spins is None else tuple(spins))
+        plist = [pos[i, : len(self._mols[i])] for i in range(nmol)]
+        if self._pb is None or self._pb_key != key:
+            self._pb = engine.PackedBatch(self.tables, self._mols, plist, self.device, chg,
+                                          [int(s) for s in spins] if spins else None)
+            self._pb_key = key
+        else:
+            self._pb.set_positions(plist)
+        res = engine.run(self._pb, etemp=self.etemp, maxiter=self.maxiter, tol=self.tol,
+                         forces=forces, gb=self.solvation, state=self._state)
+        st = res.status.cpu()
+        bad = st[(st != 0)]
+        if len(bad):
+            codes = set(bad.tolist())
+            if codes - {4}:
+                from ._lib import STATUS
+
+                raise RuntimeError(f"single point failed: {[STATUS.get(c, c) for c in codes]}")
+            if self.opts.get("force_convergence", False):
+                raise SCFConvergenceError("SCF did not converge")
+            warnings.warn("SCF did not converge within maxiter", SCFConvergenceWarning, stacklevel=3)
+        energy = res.energy if self.include_rep else res.energy - res.e_rep
+        grad = None
+        if forces:
+            g = res.gradient
+            if not self.include_rep:
+                raise NotImplementedError("gradient without repulsion")
+            grad = torch.zeros_like(pos)
+            off = self._pb.atom_off
+            for i in range(nmol):
+                grad[i, : len(self._mols[i])] = g[off[i] : off[i + 1]]
+            grad = grad.reshape(positions.shape)
+        if not self.batched:
+            energy = energy[0]
+        return {"energy": energy, "gradient": grad, "result": res}
+
+    # ---- public API (calculators/types/abc.py:88-170) ----
+    def get_energy(self, positions, chrg=0, spin=None, **_):
+        return self.energy(positions, chrg, spin)
+
+    def energy(self, positions, chrg=0, spin=None):
+        if positions.requires_grad:
+            return _Energy.apply(positions, self, chrg, spin)
+        return self._run(positions, chrg, spin)["energy"]
+
+    def get_forces(self, positions, chrg=0, spin=None, grad_mode="autograd", **_):
+        return self.forces(positions, chrg, spin)
+
+    def forces(self, positions, chrg=0, spin=None):
+        r = self._run(positions.detach(), chrg, spin, forces=True)
+        return -r["gradient"]
+
+    def singlepoint(self, positions, chrg=0, spin=None):
+        r = self._run(positions.detach(), chrg, spin)
+        res = r["result"]
+        return {
+            "energy": r["energy"],
+            "scf": res.e_scf if self.batched else res.e_scf[0],
+            "fenergy": res.e_free if self.batched else res.e_free[0],
+            "repulsion": res.e_rep if self.batched else res.e_rep[0],
+            "iterations": res.iterations,
+        }
+
+
+class GFN1Calculator(Calculator):
+    """GFN1-xTB (calculators/gfn1.py)."""
+
+    method = "gfn1"
+
+
+class GFN2Calculator(Calculator):
+    """GFN2-xTB (calculators/gfn2.py:267-298)."""
+
+    method = "gfn2"

@@ -1,0 +1,80 @@
+// Shared device helpers for the dxtb_gb300 kernels (sm_103a, float64).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/dxtb_gb300.h"
+
+#define DXTB_CHECK_LAUNCH()                                   \
+  do {                                                        \
+    cudaError_t _e = cudaGetLastError();                      \
+    if (_e != cudaSuccess) return DXTB_ERR_LAUNCH;            \
+  } while (0)
+
+namespace dxtb {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr double kEps = 2.220446049250313080847263336181640625e-16;
+constexpr double kTiny = 2.2250738585072014e-308;
+
+__device__ __forceinline__ double pf(const double *p, int off) { return __ldg(p + off); }
+__device__ __forceinline__ int pi_(const int32_t *p, int off) { return __ldg(p + off); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum; `red` is shared scratch of >= 32 doubles. All threads of
+// the block must call it; every thread receives the result.
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : -1.0e308;
+  if (wid == 0) t = warp_max(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Molecule of a flat index given a prefix array off[0..nmol] (binary search).
+__device__ __forceinline__ int find_mol(const int64_t *off, int nmol, int64_t k) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(off + mid) <= k) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace dxtb

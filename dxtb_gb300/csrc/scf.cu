@@ -1,0 +1,567 @@
+// Persistent self-consistent-field kernel: one CTA per molecule runs the
+// whole SCF of that molecule (orthogonaliser, Fock build, generalized
+// eigensolve, Fermi occupations, density, Mulliken charges and atomic
+// multipoles, potentials, Anderson mixing) with a per-molecule convergence
+// test and iteration cap. No host synchronisation inside the loop.
+//
+// Reference path (src/dxtb/_src): scf/iterator.py:51-195, scf/pure/
+// conversions.py:106-366 (charges <-> potential <-> Fock <-> density),
+// scf/pure/ovlp_diag.py:36-62 and exlibs/xitorch/_impls/linalg/symeig.py:
+// 38-76 (Cholesky orthogonaliser + symmetric eigensolver), wavefunction/
+// filling.py:428-742 (Fermi occupations), scf/utils.py:29-52 (density),
+// components/interactions/{base,list}.py and coulomb/{secondorder,
+// thirdorder,multipole}.py (potentials and energies), scf/base.py:510-619
+// (energy and electronic free energy).
+#include "linalg.cuh"
+
+namespace dxtb {
+
+constexpr int kScfThreads = 256;
+constexpr int kHist = 6;  // Anderson history length
+
+struct MolView {
+  int m, n, nat, nsh, N;
+  int64_t a0, s0, o0, moff, mtot, n2off, n2tot, g0;
+};
+
+// Per-molecule workspace layout (doubles).
+__host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
+  const int64_t N = n + 9 * nat;
+  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat;
+}
+
+struct Ws {
+  double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
+  double *vsh_tmp;
+};
+
+__device__ inline Ws ws_carve(double *base, int n, int nat) {
+  const int N = n + 9 * nat;
+  Ws w;
+  double *q = base;
+  w.Linv = q; q += (size_t)n * n;
+  w.A = q; q += (size_t)n * n;
+  w.Zt = q; q += (size_t)n * n;
+  w.d = q; q += n;
+  w.e = q; q += n;
+  w.tau = q; q += n;
+  w.p = q; q += n;
+  w.rc = q; q += n;
+  w.rs = q; q += n;
+  w.eps = q; q += n;
+  w.fa = q; q += n;
+  w.fb = q; q += n;
+  w.vsh_tmp = q; q += n;
+  w.x = q; q += N;
+  w.g = q; q += N;
+  w.hx = q; q += (size_t)kHist * N;
+  w.hr = q; q += (size_t)kHist * N;
+  w.misc = q;  // 64 + 16 nat + 2N
+  return w;
+}
+
+// Fermi-Dirac occupations of singly occupied orbitals summing to nel
+// (filling.py:428-742 converges to the same unique root). Bisection on the
+// electron count, warp 0 only. Returns false on failure.
+__device__ bool fermi_warp(int n, const double *eps, double nel, double kt, double *f) {
+  const int lane = threadIdx.x & 31;
+  if (nel <= 0.0) {
+    for (int j = lane; j < n; j += 32) f[j] = 0.0;
+    return true;
+  }
+  if (nel >= (double)n) {
+    for (int j = lane; j < n; j += 32) f[j] = 1.0;
+    return true;
+  }
+  double emin = 1e308, emax = -1e308;
+  for (int j = lane; j < n; j += 32) {
+    emin = fmin(emin, eps[j]);
+    emax = fmax(emax, eps[j]);
+  }
+  emin = -warp_max(-emin);
+  emax = warp_max(emax);
+  double lo = emin - 60.0 * kt, hi = emax + 60.0 * kt;
+  for (int it = 0; it < 200; ++it) {
+    const double mu = 0.5 * (lo + hi);
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) {
+      const double x = (eps[j] - mu) / kt;
+      s += x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+    }
+    s = warp_sum(s);
+    if (s > nel) hi = mu; else lo = mu;
+    if (hi - lo < 1e-16 * fmax(1.0, fabs(mu))) break;
+  }
+  const double mu = 0.5 * (lo + hi);
+  double s = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    const double x = (eps[j] - mu) / kt;
+    const double v = x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+    f[j] = v;
+    s += v;
+  }
+  s = warp_sum(s);
+  return fabs(s - nel) < 1e-6;
+}
+
+__device__ __forceinline__ double ent(double f) {
+  const double o = fmax(f, kEps), o1 = fmax(1.0 - f, kEps);
+  return o * log(o) + o1 * log(o1);
+}
+
+struct ScfArgs {
+  dxtb_batch b;
+  const double *pf;
+  const int32_t *pi;
+  const double *S, *H0, *D, *Q, *gamma, *hd, *sd, *dd, *sq, *gb, *n0, *nel;
+  double kt, tol;
+  int maxiter;
+  const int64_t *ws_off;
+  const int32_t *order;
+  double *ws, *P, *W, *C, *evals, *occ, *q, *dp, *qp, *vorb, *vdp, *vqp, *energies;
+  int32_t *status;
+};
+
+// Potential x = (vorb [n], vdp [nat][3], vqp [nat][6]) from the orbital
+// charges qo and atomic multipoles dpa/qpa (interactions/base.py:135-181).
+__device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, const double *qo,
+                                       const double *dpa, const double *qpa, double *qsh,
+                                       double *qat, double *vsh, double *vat, double *xout,
+                                       int multipole, int es3_shell) {
+  const dxtb_batch &b = a.b;
+  const int n = mv.n, nat = mv.nat, nsh = mv.nsh;
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    const int t = b.shell_type[mv.s0 + s];
+    const int o = b.shell_ao[mv.s0 + s], no = 2 * pi_(a.pi, DXTB_I_L + t) + 1;
+    double v = 0.0;
+    for (int k = 0; k < no; ++k) v += qo[o + k];
+    qsh[s] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nat; i += blockDim.x) qat[i] = 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int s = 0; s < nsh; ++s) qat[b.shell_atom[mv.s0 + s]] += qsh[s];
+  __syncthreads();
+  // shell potential: ES2 gamma q_sh (+ shell-resolved ES3)
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    const double *gr = a.gamma + mv.g0 + (size_t)s * nsh;
+    double v = 0.0;
+    for (int t = 0; t < nsh; ++t) v = fma(gr[t], qsh[t], v);
+    if (es3_shell) v += a.hd[mv.s0 + s] * qsh[s] * qsh[s];
+    vsh[s] = v;
+  }
+  // atom potential: atom-resolved ES3, AES2 monopole terms, GB
+  for (int i = threadIdx.x; i < nat; i += blockDim.x) {
+    double v = es3_shell ? 0.0 : a.hd[mv.a0 + i] * qat[i] * qat[i];
+    if (multipole) {
+      for (int j = 0; j < nat; ++j) {
+        const int64_t o = mv.n2off + (int64_t)i * nat + j;
+        for (int c = 0; c < 3; ++c) v += a.sd[c * mv.n2tot + o] * dpa[3 * j + c];
+        for (int c = 0; c < 6; ++c) v += a.sq[c * mv.n2tot + o] * qpa[6 * j + c];
+      }
+    }
+    if (a.gb != nullptr) {
+      const double *gr = a.gb + mv.n2off + (size_t)i * nat;
+      for (int j = 0; j < nat; ++j) v += gr[j] * qat[j];
+    }
+    vat[i] = v;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+    const int s = b.ao_shell[mv.o0 + o];
+    xout[o] = vsh[s] + vat[b.shell_atom[mv.s0 + s]];
+  }
+  if (multipole) {
+    const double qscale[6] = {1.0, 2.0, 1.0, 2.0, 2.0, 1.0};
+    for (int j = threadIdx.x; j < nat; j += blockDim.x) {
+      const int zj = b.numbers[mv.a0 + j];
+      const double dk = pf(a.pf, DXTB_P_DKERNEL + zj), qk = pf(a.pf, DXTB_P_QKERNEL + zj);
+      double vd[3], vq[6];
+      for (int c = 0; c < 3; ++c) vd[c] = 2.0 * dk * dpa[3 * j + c];
+      for (int c = 0; c < 6; ++c) vq[c] = 2.0 * qk * qpa[6 * j + c] * qscale[c];
+      for (int i = 0; i < nat; ++i) {
+        const int64_t o = mv.n2off + (int64_t)i * nat + j;
+        for (int c = 0; c < 3; ++c) vd[c] += a.sd[c * mv.n2tot + o] * qat[i];
+        for (int x = 0; x < 3; ++x)
+          for (int y = 0; y < 3; ++y) vd[y] += a.dd[(3 * x + y) * mv.n2tot + o] * dpa[3 * i + x];
+        for (int c = 0; c < 6; ++c) vq[c] += a.sq[c * mv.n2tot + o] * qat[i];
+      }
+      for (int c = 0; c < 3; ++c) xout[n + 3 * j + c] = vd[c];
+      for (int c = 0; c < 6; ++c) xout[n + 3 * nat + 6 * j + c] = vq[c];
+    }
+  }
+  __syncthreads();
+}
+
+// Interaction energy (interactions/base.py:306-360 summed): block result.
+__device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const double *qsh,
+                                     const double *qat, const double *dpa, const double *qpa,
+                                     int multipole, int es3_shell, double *red) {
+  const dxtb_batch &b = a.b;
+  const int nat = mv.nat, nsh = mv.nsh;
+  double e = 0.0;
+  for (int s = threadIdx.x; s < nsh; s += blockDim.x) {
+    const double *gr = a.gamma + mv.g0 + (size_t)s * nsh;
+    double v = 0.0;
+    for (int t = 0; t < nsh; ++t) v = fma(gr[t], qsh[t], v);
+    e += 0.5 * qsh[s] * v;
+    if (es3_shell) e += a.hd[mv.s0 + s] * qsh[s] * qsh[s] * qsh[s] / 3.0;
+  }
+  const double qscale[6] = {1.0, 2.0, 1.0, 2.0, 2.0, 1.0};
+  for (int j = threadIdx.x; j < nat; j += blockDim.x) {
+    if (!es3_shell) e += a.hd[mv.a0 + j] * qat[j] * qat[j] * qat[j] / 3.0;
+    if (multipole) {
+      const int zj = b.numbers[mv.a0 + j];
+      const double dk = pf(a.pf, DXTB_P_DKERNEL + zj), qk = pf(a.pf, DXTB_P_QKERNEL + zj);
+      double vd[3] = {0, 0, 0}, vq[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = 0; i < nat; ++i) {
+        const int64_t o = mv.n2off + (int64_t)i * nat + j;
+        for (int c = 0; c < 3; ++c) vd[c] += a.sd[c * mv.n2tot + o] * qat[i];
+        for (int x = 0; x < 3; ++x)
+          for (int y = 0; y < 3; ++y)
+            vd[y] += 0.5 * a.dd[(3 * x + y) * mv.n2tot + o] * dpa[3 * i + x];
+        for (int c = 0; c < 6; ++c) vq[c] += a.sq[c * mv.n2tot + o] * qat[i];
+      }
+      for (int c = 0; c < 3; ++c) e += (dk * dpa[3 * j + c] + vd[c]) * dpa[3 * j + c];
+      for (int c = 0; c < 6; ++c) e += (qk * qscale[c] * qpa[6 * j + c] + vq[c]) * qpa[6 * j + c];
+    }
+    if (a.gb != nullptr) {
+      const double *gr = a.gb + mv.n2off + (size_t)j * nat;
+      double v = 0.0;
+      for (int i = 0; i < nat; ++i) v += gr[i] * qat[i];
+      e += 0.5 * qat[j] * v;
+    }
+  }
+  return block_sum(e, red);
+}
+
+__global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
+  __shared__ double red[32];
+  __shared__ int s_flag;
+  const dxtb_batch &b = a.b;
+  MolView mv;
+  mv.m = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+  const int m = mv.m;
+  mv.a0 = b.atom_off[m];
+  mv.s0 = b.shell_off[m];
+  mv.o0 = b.ao_off[m];
+  mv.moff = b.mat_off[m];
+  mv.mtot = b.mat_off[b.nmol];
+  mv.n2off = b.nat2_off[m];
+  mv.n2tot = b.nat2_off[b.nmol];
+  mv.g0 = b.nsh2_off[m];
+  mv.n = (int)(b.ao_off[m + 1] - mv.o0);
+  mv.nat = (int)(b.atom_off[m + 1] - mv.a0);
+  mv.nsh = (int)(b.shell_off[m + 1] - mv.s0);
+  const int n = mv.n, nat = mv.nat;
+  const int multipole = pi_(a.pi, DXTB_I_SCAL + DXTB_IS_MULTIPOLE);
+  const int es3_shell = pi_(a.pi, DXTB_I_SCAL + DXTB_IS_ES3_SHELL);
+  const int N = n + (multipole ? 9 * nat : 0);
+  mv.N = N;
+  Ws w = ws_carve(a.ws + a.ws_off[m], n, nat);
+  double *qsh = w.misc, *qat = qsh + mv.nsh + 1, *vat = qat + nat + 1;
+  double *dpa = vat + nat + 1, *qpa = dpa + 3 * nat + 1, *qo = qpa + 6 * nat + 1;
+  double *amat = qo + n + 1;  // Anderson normal equations (kHist^2 + kHist)
+  double *vsh = w.vsh_tmp;
+
+  const double *S = a.S + mv.moff, *H0 = a.H0 + mv.moff;
+  double *P = a.P + mv.moff, *C = a.C + mv.moff;
+  const double *n0 = a.n0 + mv.o0;
+  const double nel_a = a.nel[2 * m], nel_b = a.nel[2 * m + 1];
+  int status = DXTB_OK;
+
+  // ---- orthogonaliser X = L^-1 (S = L L^T), once per geometry ----
+  for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = S[t];
+  __syncthreads();
+  if (!cta_cholesky(n, w.A, red)) status = DXTB_ERR_NOT_POSDEF;
+  if (status == DXTB_OK) cta_trinv(n, w.A, w.Linv);
+
+  for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = 0.0;
+  __syncthreads();
+
+  int it = 0, nhist = 0, hpos = 0;
+  double resid = 0.0;
+  const double beta_mix = 0.4;
+  while (status == DXTB_OK) {
+    ++it;
+    // ---- Fock matrix F(x) into Zt (conversions.py:255-297) ----
+    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+      const int i = (int)(t / n), j = (int)(t % n);
+      double f = H0[t] - 0.5 * S[t] * (w.x[i] + w.x[j]);
+      if (multipole) {
+        const int ai = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + i]];
+        const int aj = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + j]];
+        const int64_t e1 = mv.moff + t, e2 = mv.moff + (int64_t)j * n + i;
+        double acc = 0.0;
+        for (int c = 0; c < 3; ++c)
+          acc += a.D[c * mv.mtot + e1] * w.x[n + 3 * aj + c] + a.D[c * mv.mtot + e2] * w.x[n + 3 * ai + c];
+        for (int c = 0; c < 6; ++c)
+          acc += a.Q[c * mv.mtot + e1] * w.x[n + 3 * nat + 6 * aj + c] +
+                 a.Q[c * mv.mtot + e2] * w.x[n + 3 * nat + 6 * ai + c];
+        f -= 0.5 * acc;
+      }
+      w.Zt[t] = f;
+    }
+    __syncthreads();
+    // ---- F' = X F X^T (exlibs/xitorch/_impls/linalg/symeig.py:57-61) ----
+    cta_gemm<false, false>(n, n, n, 1.0, w.Linv, n, w.Zt, n, 0.0, w.A, n);   // A = X F
+    cta_gemm<false, true>(n, n, n, 1.0, w.A, n, w.Linv, n, 0.0, w.Zt, n);    // Zt = (X F) X^T
+    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = w.Zt[t];
+    __syncthreads();
+    // ---- eigensolve: Householder tridiagonalisation + implicit QL ----
+    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, red);
+    cta_form_q(n, w.A, w.tau, C, w.Zt, w.p);  // C used as scratch
+    if (!cta_tql(n, w.d, w.e, w.Zt, w.rc, w.rs)) {
+      status = DXTB_ERR_NAN;
+      break;
+    }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) w.eps[j] = w.d[j];
+    // ---- C^T = Zt X (orbital j is row j) ----
+    cta_gemm<false, false>(n, n, n, 1.0, w.Zt, n, w.Linv, n, 0.0, C, n);
+    // ---- Fermi occupations (filling.py:428-742), both spin channels ----
+    if (threadIdx.x < 32) {
+      bool ok = fermi_warp(n, w.eps, nel_a, a.kt, w.fa);
+      ok = ok && fermi_warp(n, w.eps, nel_b, a.kt, w.fb);
+      if (threadIdx.x == 0) s_flag = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_flag) {
+      status = DXTB_ERR_FERMI;
+      break;
+    }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) w.p[j] = w.fa[j] + w.fb[j];
+    __syncthreads();
+    // ---- density P = C diag(occ) C^T (scf/utils.py:29-52) ----
+    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = C[t] * w.p[t / n];
+    __syncthreads();
+    cta_gemm<true, false>(n, n, n, 1.0, C, n, w.A, n, 0.0, P, n);
+    // ---- Mulliken charges and atomic multipoles (conversions.py:203-251) ----
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double pop = 0.0;
+      for (int k = 0; k < n; ++k) pop = fma(P[(size_t)k * n + i], S[(size_t)k * n + i], pop);
+      qo[i] = n0[i] - pop;
+    }
+    if (multipole) {
+      for (int t = threadIdx.x; t < 3 * nat; t += blockDim.x) dpa[t] = 0.0;
+      for (int t = threadIdx.x; t < 6 * nat; t += blockDim.x) qpa[t] = 0.0;
+      __syncthreads();
+      // -sum_k P_ik M[c][k][i] per orbital i, reduced onto the atom of i
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double acc[9];
+        for (int c = 0; c < 9; ++c) acc[c] = 0.0;
+        for (int k = 0; k < n; ++k) {
+          const double pk = P[(size_t)k * n + i];
+          const int64_t e = mv.moff + (int64_t)k * n + i;
+          for (int c = 0; c < 3; ++c) acc[c] -= pk * a.D[c * mv.mtot + e];
+          for (int c = 0; c < 6; ++c) acc[3 + c] -= pk * a.Q[c * mv.mtot + e];
+        }
+        const int ai = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + i]];
+        for (int c = 0; c < 3; ++c) atomicAdd(&dpa[3 * ai + c], acc[c]);
+        for (int c = 0; c < 6; ++c) atomicAdd(&qpa[6 * ai + c], acc[3 + c]);
+      }
+    }
+    __syncthreads();
+    // ---- new potential G(x) ----
+    potential_from_charges(a, mv, qo, dpa, qpa, qsh, qat, vsh, vat, w.g, multipole, es3_shell);
+    double part = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) part = fmax(part, fabs(w.g[t] - w.x[t]));
+    resid = block_max(part, red);
+    if (resid < a.tol) break;
+    if (it >= a.maxiter) {
+      status = DXTB_ERR_MAXITER;
+      break;
+    }
+    // ---- Anderson mixing of the potential (scf/mixer/anderson.py) ----
+    // history: hx[k] = x_k, hr[k] = r_k = G(x_k) - x_k (ring buffer)
+    double *hxk = w.hx + (size_t)hpos * N, *hrk = w.hr + (size_t)hpos * N;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      hxk[t] = w.x[t];
+      hrk[t] = w.g[t] - w.x[t];
+    }
+    __syncthreads();
+    nhist = min(nhist + 1, kHist);
+    const int newest = hpos;
+    hpos = (hpos + 1) % kHist;
+    const int mm = nhist - 1;  // number of differences
+    if (mm == 0) {
+      for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] += beta_mix * hrk[t];
+    } else {
+      // differences relative to the newest: dR_k = r_newest - r_k, dX_k = x_newest - x_k
+      // normal equations (dR^T dR) gam = dR^T r_newest
+      int idx[kHist];
+      int c = 0;
+      for (int k = 0; k < kHist && c < mm; ++k) {
+        const int slot = (newest - 1 - k + 2 * kHist) % kHist;
+        idx[c++] = slot;
+      }
+      for (int u = 0; u < mm; ++u) {
+        const double *ru = w.hr + (size_t)idx[u] * N;
+        for (int v = u; v <= mm; ++v) {
+          const double *rv = v < mm ? w.hr + (size_t)idx[v] * N : nullptr;
+          double s = 0.0;
+          for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            const double du = hrk[t] - ru[t];
+            const double dv = v < mm ? hrk[t] - rv[t] : hrk[t];
+            s += du * dv;
+          }
+          s = block_sum(s, red);
+          if (threadIdx.x == 0) {
+            if (v < mm) {
+              amat[u * kHist + v] = s;
+              amat[v * kHist + u] = s;
+            } else {
+              amat[kHist * kHist + u] = s;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        // Gaussian elimination with partial pivoting, Tikhonov shift
+        double M[kHist][kHist + 1];
+        double tr = 0.0;
+        for (int u = 0; u < mm; ++u) tr += amat[u * kHist + u];
+        for (int u = 0; u < mm; ++u) {
+          for (int v = 0; v < mm; ++v) M[u][v] = amat[u * kHist + v];
+          M[u][u] += 1e-12 * tr + 1e-300;
+          M[u][mm] = amat[kHist * kHist + u];
+        }
+        for (int col = 0; col < mm; ++col) {
+          int piv = col;
+          for (int r = col + 1; r < mm; ++r)
+            if (fabs(M[r][col]) > fabs(M[piv][col])) piv = r;
+          for (int v = 0; v <= mm; ++v) {
+            const double tmp = M[col][v];
+            M[col][v] = M[piv][v];
+            M[piv][v] = tmp;
+          }
+          for (int r = col + 1; r < mm; ++r) {
+            const double f = M[r][col] / M[col][col];
+            for (int v = col; v <= mm; ++v) M[r][v] -= f * M[col][v];
+          }
+        }
+        for (int r = mm - 1; r >= 0; --r) {
+          double s = M[r][mm];
+          for (int v = r + 1; v < mm; ++v) s -= M[r][v] * amat[kHist * kHist + kHist + v];
+          amat[kHist * kHist + kHist + r] = s / M[r][r];
+        }
+      }
+      __syncthreads();
+      const double *gam = amat + kHist * kHist + kHist;
+      for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        double xn = w.x[t] + beta_mix * hrk[t];
+        for (int u = 0; u < mm; ++u) {
+          const double *xu = w.hx + (size_t)idx[u] * N, *ru = w.hr + (size_t)idx[u] * N;
+          xn -= gam[u] * ((w.x[t] - xu[t]) + beta_mix * (hrk[t] - ru[t]));
+        }
+        w.x[t] = xn;
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- outputs ----
+  if (status == DXTB_OK || status == DXTB_ERR_MAXITER) {
+    // energies (scf/base.py:510-619): E_h0 + E_int and -TS
+    double part = 0.0;
+    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) part += P[t] * H0[t];
+    const double eh0 = block_sum(part, red);
+    const double eint = interaction_energy(a, mv, qsh, qat, dpa, qpa, multipole, es3_shell, red);
+    double ts = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) ts += ent(w.fa[j]) + ent(w.fb[j]);
+    ts = a.kt * block_sum(ts, red);
+    if (threadIdx.x == 0) {
+      a.energies[4 * m + 0] = eh0 + eint;
+      a.energies[4 * m + 1] = ts;
+      a.energies[4 * m + 2] = (double)it;
+      a.energies[4 * m + 3] = resid;
+      if (!isfinite(eh0 + eint + ts)) status = DXTB_ERR_NAN;
+    }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      a.evals[mv.o0 + j] = w.eps[j];
+      a.occ[mv.o0 + j] = w.fa[j] + w.fb[j];
+      a.q[mv.o0 + j] = qo[j];
+    }
+    // potentials of the final charges (for the gradient)
+    for (int t = threadIdx.x; t < n; t += blockDim.x) a.vorb[mv.o0 + t] = w.g[t];
+    if (multipole) {
+      for (int t = threadIdx.x; t < 3 * nat; t += blockDim.x) {
+        a.vdp[3 * mv.a0 + t] = w.g[n + t];
+        a.dp[3 * mv.a0 + t] = dpa[t];
+      }
+      for (int t = threadIdx.x; t < 6 * nat; t += blockDim.x) {
+        a.vqp[6 * mv.a0 + t] = w.g[n + 3 * nat + t];
+        a.qp[6 * mv.a0 + t] = qpa[t];
+      }
+    }
+    // energy-weighted density W = C diag(occ eps) C^T
+    if (a.W != nullptr) {
+      for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x)
+        w.A[t] = C[t] * (w.fa[t / n] + w.fb[t / n]) * w.eps[t / n];
+      __syncthreads();
+      cta_gemm<true, false>(n, n, n, 1.0, C, n, w.A, n, 0.0, a.W + mv.moff, n);
+    }
+  }
+  if (threadIdx.x == 0) a.status[m] = status;
+}
+
+}  // namespace dxtb
+
+using namespace dxtb;
+
+extern "C" int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat) { return ws_size_mol(n, nat); }
+
+extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
+                            const double *overlap, const double *h0, const double *dipole,
+                            const double *quadrupole, const double *gamma, const double *hd,
+                            const double *amat_sd, const double *amat_dd, const double *amat_sq,
+                            const double *gb_mat, const double *n0, const double *nel, double kt,
+                            int32_t maxiter, double tol, const int64_t *ws_off,
+                            const int32_t *order, double *workspace, double *density,
+                            double *wdensity, double *coeff, double *evals, double *occ, double *q,
+                            double *dp, double *qp, double *vorb, double *vdp, double *vqp,
+                            double *energies, int32_t *status, void *stream) {
+  if (!b || b->nmol <= 0 || !overlap || !h0 || !gamma || !hd || !n0 || !nel || !ws_off ||
+      !workspace || !density || !coeff || !evals || !occ || !q || !vorb || !energies || !status)
+    return DXTB_ERR_ARGS;
+  if (maxiter <= 0 || !(kt > 0.0)) return DXTB_ERR_ARGS;
+  ScfArgs a;
+  a.b = *b;
+  a.pf = par_f;
+  a.pi = par_i;
+  a.S = overlap;
+  a.H0 = h0;
+  a.D = dipole;
+  a.Q = quadrupole;
+  a.gamma = gamma;
+  a.hd = hd;
+  a.sd = amat_sd;
+  a.dd = amat_dd;
+  a.sq = amat_sq;
+  a.gb = gb_mat;
+  a.n0 = n0;
+  a.nel = nel;
+  a.kt = kt;
+  a.tol = tol;
+  a.maxiter = maxiter;
+  a.ws_off = ws_off;
+  a.order = order;
+  a.ws = workspace;
+  a.P = density;
+  a.W = wdensity;
+  a.C = coeff;
+  a.evals = evals;
+  a.occ = occ;
+  a.q = q;
+  a.dp = dp;
+  a.qp = qp;
+  a.vorb = vorb;
+  a.vdp = vdp;
+  a.vqp = vqp;
+  a.energies = energies;
+  a.status = status;
+  k_scf<<<b->nmol, kScfThreads, 0, (cudaStream_t)stream>>>(a);
+  DXTB_CHECK_LAUNCH();
+  return DXTB_OK;
+}

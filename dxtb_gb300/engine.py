@@ -1,0 +1,290 @@
+"""
+Packed ragged batches and the device pipeline of one GFN-xTB single point.
+
+A batch of molecules of uneven size is packed without padding (offset tables
+per molecule for atoms, shells, orbitals and the n^2 / nat^2 / nsh^2 blocks),
+uploaded once, and pushed through the CUDA library:
+
+    coordination numbers -> interaction caches -> multipole integrals + H0
+    -> persistent SCF (all molecules, one launch) -> analytic gradient.
+
+All device memory is owned by PyTorch (caching allocator); the kernels
+allocate nothing. Everything runs on the caller's current CUDA stream.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import Tables
+
+F64 = torch.float64
+
+
+def _prefix(v: np.ndarray) -> np.ndarray:
+    out = np.zeros(len(v) + 1, dtype=np.int64)
+    np.cumsum(v, out=out[1:])
+    return out
+
+
+def alpha_beta(nel: float, spin: int | None = None) -> tuple[float, float]:
+    """Alpha/beta electrons (wavefunction/filling.py:180-259)."""
+    if spin is None:
+        uhf = math.floor(nel + 0.5) % 2
+    else:
+        uhf = int(spin)
+        if uhf % 2 != math.floor(nel + 0.5) % 2:
+            uhf = math.floor(nel + 0.5) % 2
+    diff = min(uhf, nel)
+    nb = (nel - diff) / 2.0
+    return nb + diff, nb
+
+
+class PackedBatch:
+    """Device-resident packed layout of a list of molecules."""
+
+    def __init__(self, tables: Tables, numbers: list, positions: list, device=None,
+                 charges=None, spins=None):
+        device = torch.device(device or "cuda")
+        self.device = device
+        self.tables = tables
+        nums = [np.asarray(n.cpu() if torch.is_tensor(n) else n, dtype=np.int64).ravel() for n in numbers]
+        nums = [n[n > 0] for n in nums]
+        for n in nums:
+            tables.check_elements(n)
+        self.nmol = len(nums)
+        if self.nmol == 0:
+            raise ValueError("empty batch")
+        L = tables.i32
+        from .params import layout
+
+        lay = layout()
+        sh0 = L[lay["DXTB_I_EL_SH0"] : lay["DXTB_I_EL_SH0"] + lay["DXTB_MAXZ"]]
+        nshe = L[lay["DXTB_I_EL_NSH"] : lay["DXTB_I_EL_NSH"] + lay["DXTB_MAXZ"]]
+        lt = L[lay["DXTB_I_L"] : lay["DXTB_I_L"] + lay["DXTB_MAXSHT"]]
+        refocc = tables.f64[lay["DXTB_P_REFOCC"] : lay["DXTB_P_REFOCC"] + lay["DXTB_MAXSHT"]]
+
+        nat = np.array([len(n) for n in nums], dtype=np.int64)
+        sh_atom, sh_type, sh_ao, ao_sh, n0 = [], [], [], [], []
+        nsh, nao, nel = [], [], []
+        for mi, z in enumerate(nums):
+            cnt = nshe[z]
+            st = np.concatenate([sh0[zz] + np.arange(c) for zz, c in zip(z, cnt)]).astype(np.int32)
+            sa = np.repeat(np.arange(len(z), dtype=np.int32), cnt)
+            no = 2 * lt[st] + 1
+            so = (np.cumsum(no) - no).astype(np.int32)
+            aos = np.repeat(np.arange(len(st), dtype=np.int32), no)
+            sh_atom.append(sa)
+            sh_type.append(st)
+            sh_ao.append(so)
+            ao_sh.append(aos)
+            n0.append(np.repeat(refocc[st] / no, no))
+            nsh.append(len(st))
+            nao.append(int(no.sum()))
+            ch = 0.0 if charges is None else float(charges[mi])
+            ne = float(refocc[st].sum()) - ch
+            sp = None if spins is None else spins[mi]
+            nel.append(alpha_beta(ne, sp))
+        nsh = np.array(nsh, dtype=np.int64)
+        nao = np.array(nao, dtype=np.int64)
+        self.nat, self.nsh, self.nao = nat, nsh, nao
+        self.atom_off = _prefix(nat)
+        self.shell_off = _prefix(nsh)
+        self.ao_off = _prefix(nao)
+        self.mat_off = _prefix(nao * nao)
+        self.nat2_off = _prefix(nat * nat)
+        self.nsh2_off = _prefix(nsh * nsh)
+        self.pair_off = _prefix(nsh * (nsh + 1) // 2)
+        ws = np.array([_lib.lib().dxtb_scf_workspace_mol(int(n), int(a)) for n, a in zip(nao, nat)])
+        self.ws_off = _prefix(ws)
+
+        def dev(a, dt):
+            return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(device, non_blocking=False)
+
+        self.t = {
+            "atom_off": dev(self.atom_off, torch.int64),
+            "shell_off": dev(self.shell_off, torch.int64),
+            "ao_off": dev(self.ao_off, torch.int64),
+            "mat_off": dev(self.mat_off, torch.int64),
+            "nat2_off": dev(self.nat2_off, torch.int64),
+            "nsh2_off": dev(self.nsh2_off, torch.int64),
+            "pair_off": dev(self.pair_off, torch.int64),
+            "ws_off": dev(self.ws_off, torch.int64),
+            "numbers": dev(np.concatenate(nums), torch.int32),
+            "shell_atom": dev(np.concatenate(sh_atom), torch.int32),
+            "shell_type": dev(np.concatenate(sh_type), torch.int32),
+            "shell_ao": dev(np.concatenate(sh_ao), torch.int32),
+            "ao_shell": dev(np.concatenate(ao_sh), torch.int32),
+            "n0": dev(np.concatenate(n0), F64),
+            "nel": dev(np.array(nel, dtype=np.float64), F64),
+            "order": dev(np.argsort(-nao, kind="stable").astype(np.int32), torch.int32),
+            "par_f": dev(tables.f64, F64),
+            "par_i": dev(tables.i32, torch.int32),
+        }
+        self.numbers = nums
+        self.set_positions(positions)
+
+    def set_positions(self, positions: list) -> None:
+        pos = [torch.as_tensor(p, dtype=F64).reshape(-1, 3) for p in positions]
+        pos = [p[: int(self.nat[i])] for i, p in enumerate(pos)]
+        self.positions = torch.cat([p.to(self.device) for p in pos]).contiguous()
+        self._struct = None
+
+    @property
+    def struct(self) -> _lib.Batch:
+        if self._struct is None:
+            t = self.t
+            self._struct = _lib.Batch(
+                self.nmol, int(self.nao.max()), int(self.nat.max()), int(self.nsh.max()),
+                t["atom_off"].data_ptr(), t["shell_off"].data_ptr(), t["ao_off"].data_ptr(),
+                t["mat_off"].data_ptr(), t["nat2_off"].data_ptr(), t["nsh2_off"].data_ptr(),
+                t["pair_off"].data_ptr(), t["numbers"].data_ptr(), self.positions.data_ptr(),
+                t["shell_atom"].data_ptr(), t["shell_type"].data_ptr(), t["shell_ao"].data_ptr(),
+                t["ao_shell"].data_ptr(),
+            )
+        return self._struct
+
+    @property
+    def total(self) -> dict:
+        return {
+            "atoms": int(self.atom_off[-1]), "shells": int(self.shell_off[-1]),
+            "aos": int(self.ao_off[-1]), "mat": int(self.mat_off[-1]),
+            "nat2": int(self.nat2_off[-1]), "nsh2": int(self.nsh2_off[-1]),
+            "ws": int(self.ws_off[-1]),
+        }
+
+
+@dataclass
+class Result:
+    energy: torch.Tensor           # [nmol] total energy (Eh)
+    e_scf: torch.Tensor            # [nmol] E_h0 + E_interactions
+    e_free: torch.Tensor           # [nmol] -TS
+    e_rep: torch.Tensor            # [nmol] repulsion
+    iterations: torch.Tensor       # [nmol]
+    status: torch.Tensor           # [nmol] int32
+    gradient: torch.Tensor | None  # [natoms, 3] packed
+    state: dict
+
+
+def _seg_sum(values: torch.Tensor, off: np.ndarray, nmol: int) -> torch.Tensor:
+    idx = torch.repeat_interleave(
+        torch.arange(nmol, device=values.device),
+        torch.as_tensor(np.diff(off), device=values.device),
+    )
+    return torch.zeros(nmol, dtype=values.dtype, device=values.device).index_add_(0, idx, values)
+
+
+def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float = 1e-10,
+        forces: bool = False, gb: dict | None = None, state: dict | None = None) -> Result:
+    """One single point for every molecule of the packed batch."""
+    L = _lib.lib()
+    from .data import radii
+
+    tb = pb.tables
+    dev = pb.device
+    tot = pb.total
+    st = _lib.stream_ptr()
+    b = C.byref(pb.struct)
+    pf, pi = pb.t["par_f"].data_ptr(), pb.t["par_i"].data_ptr()
+    s = state if state is not None else {}
+
+    def buf(key, n):
+        t = s.get(key)
+        if t is None or t.numel() < n:
+            t = torch.empty(max(n, 1), dtype=F64, device=dev)
+            s[key] = t
+        return t
+
+    na, ns, no, nm, n2, g2 = tot["atoms"], tot["shells"], tot["aos"], tot["mat"], tot["nat2"], tot["nsh2"]
+    mp = tb.multipole
+    cn = buf("cn", na)
+    _lib.check(L.dxtb_coordination_number(b, pf, pi, tb.cn_kind, cn.data_ptr(), st), "coordination number")
+    cn_mp = cn
+    if mp and tb.cn_kind != 1:
+        cn_mp = buf("cn_mp", na)
+        _lib.check(L.dxtb_coordination_number(b, pf, pi, 1, cn_mp.data_ptr(), st), "coordination number")
+    gamma, hd = buf("gamma", g2), buf("hd", ns if tb.es3_shell else na)
+    erep = buf("erep", na)
+    mrad = buf("mrad", na) if mp else None
+    sd = buf("sd", 3 * n2) if mp else None
+    dd = buf("dd", 9 * n2) if mp else None
+    sq = buf("sq", 6 * n2) if mp else None
+    _lib.check(
+        L.dxtb_interaction_cache(b, pf, pi, cn_mp.data_ptr(), gamma.data_ptr(), hd.data_ptr(),
+                                 _lib.ptr(mrad), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq),
+                                 erep.data_ptr(), st),
+        "interaction cache",
+    )
+    gbm = None
+    if gb is not None:
+        gbm = buf("gb", n2)
+        born = buf("born", na)
+        _lib.check(
+            L.dxtb_born_matrix(b, pf, pi, float(gb["epsilon"]), float(gb.get("born_scale", 1.0)),
+                               float(gb.get("born_offset", 0.0)), float(gb.get("kernel", 0)),
+                               born.data_ptr(), gbm.data_ptr(), buf("psi", na).data_ptr(), st),
+            "generalized Born",
+        )
+    S, H = buf("S", nm), buf("H", nm)
+    D = buf("D", 3 * nm) if mp else None
+    Q = buf("Q", 6 * nm) if mp else None
+    _lib.check(L.dxtb_multipole_h0(b, pf, pi, cn.data_ptr(), S.data_ptr(), H.data_ptr(),
+                                   _lib.ptr(D), _lib.ptr(Q), st), "multipole integrals")
+    P, Cm = buf("P", nm), buf("C", nm)
+    W = buf("W", nm) if forces else None
+    ev, occ, q = buf("evals", no), buf("occ", no), buf("q", no)
+    vorb = buf("vorb", no)
+    dp, qp = buf("dp", 3 * na), buf("qp", 6 * na)
+    vdp, vqp = buf("vdp", 3 * na), buf("vqp", 6 * na)
+    en = buf("energies", 4 * pb.nmol)
+    status = s.get("status")
+    if status is None or status.numel() < pb.nmol:
+        status = torch.empty(pb.nmol, dtype=torch.int32, device=dev)
+        s["status"] = status
+    ws = buf("ws", tot["ws"])
+    kt = etemp * radii.KELVIN2AU
+    _lib.check(
+        L.dxtb_scf(b, pf, pi, S.data_ptr(), H.data_ptr(), _lib.ptr(D), _lib.ptr(Q), gamma.data_ptr(),
+                   hd.data_ptr(), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq), _lib.ptr(gbm),
+                   pb.t["n0"].data_ptr(), pb.t["nel"].data_ptr(), kt, int(maxiter), float(tol),
+                   pb.t["ws_off"].data_ptr(), pb.t["order"].data_ptr(), ws.data_ptr(), P.data_ptr(),
+                   _lib.ptr(W), Cm.data_ptr(), ev.data_ptr(), occ.data_ptr(), q.data_ptr(),
+                   dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(), vdp.data_ptr(), vqp.data_ptr(),
+                   en.data_ptr(), status.data_ptr(), st),
+        "SCF",
+    )
+    e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
+    e_rep = _seg_sum(erep[:na], pb.atom_off, pb.nmol)
+    grad = None
+    if forces:
+        grad = buf("grad", 3 * na)
+        grad.zero_()
+        dedcn = buf("dedcn", na)
+        dedcn_mp = buf("dedcn_mp", na) if mp else None
+        dedcn.zero_()
+        if dedcn_mp is not None:
+            dedcn_mp.zero_()
+        _lib.check(
+            L.dxtb_gradient(b, pf, pi, cn.data_ptr(), cn_mp.data_ptr(), _lib.ptr(mrad), P.data_ptr(),
+                            W.data_ptr(), q.data_ptr(), dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(),
+                            vdp.data_ptr(), vqp.data_ptr(), S.data_ptr(), _lib.ptr(D), None, None,
+                            dedcn.data_ptr(), _lib.ptr(dedcn_mp), grad.data_ptr(), st),
+            "gradient",
+        )
+        if gb is not None:
+            _lib.check(
+                L.dxtb_born_gradient(b, pf, pi, q.data_ptr(), s["born"].data_ptr(), s["psi"].data_ptr(),
+                                     gbm.data_ptr(), None, None, float(gb["epsilon"]),
+                                     float(gb.get("born_scale", 1.0)), float(gb.get("born_offset", 0.0)),
+                                     float(gb.get("kernel", 0)), grad.data_ptr(), None, st),
+                "generalized Born gradient",
+            )
+        grad = grad[: 3 * na].view(na, 3)
+    energy = e4[:, 0] + e4[:, 1] + e_rep
+    return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], status[: pb.nmol], grad, s)

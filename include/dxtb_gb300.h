@@ -1,0 +1,246 @@
+/*
+ * dxtb_gb300 — C ABI of the GB300 (sm_103a) GFN1/GFN2-xTB single-point path.
+ *
+ * Every entry point takes plain device pointers and sizes, runs on the CUDA
+ * stream it is given, allocates nothing, and returns an int32 status
+ * (DXTB_OK or one of the DXTB_ERR_* codes). All floating-point data is
+ * float64; all index data is int32 or int64 as declared.
+ *
+ * Batches are PACKED, not padded: molecule m owns atoms
+ * [atom_off[m], atom_off[m+1]), shells [shell_off[m], shell_off[m+1]),
+ * orbitals [ao_off[m], ao_off[m+1]), a dense n_m x n_m block of every AO
+ * matrix at mat_off[m] (row-major, n_m = ao_off[m+1]-ao_off[m]), a
+ * nat_m x nat_m block of every atom-pair matrix at nat2_off[m] and a
+ * nsh_m x nsh_m block of the shell-resolved Coulomb matrix at nsh2_off[m].
+ * Multi-component AO matrices (dipole: 3, quadrupole: 6) are stored
+ * component-major: component k of molecule m starts at
+ * k * mat_off[nmol] + mat_off[m].
+ *
+ * Reference interfaces these entry points replace (paths relative to
+ * src/dxtb/_src of marvinfriede/dxtb) are cited at each declaration.
+ */
+#ifndef DXTB_GB300_H
+#define DXTB_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DXTB_OK 0
+#define DXTB_ERR_ARGS 1          /* invalid sizes or null pointers          */
+#define DXTB_ERR_LAUNCH 2        /* CUDA launch or runtime error            */
+#define DXTB_ERR_NOT_POSDEF 3    /* overlap matrix not positive definite     */
+#define DXTB_ERR_MAXITER 4       /* SCF did not converge within maxiter      */
+#define DXTB_ERR_FERMI 5         /* Fermi level search failed                */
+#define DXTB_ERR_NAN 6           /* NaN/Inf in a per-molecule result         */
+#define DXTB_ERR_TOO_LARGE 7     /* size beyond a compiled-in maximum        */
+
+/* ---- parameter tables ---------------------------------------------------
+ * Flat float64 / int32 arrays filled by the host from the GFN parameter
+ * files (param/gfn{1,2}/*.toml). A "shell type" is one shell of one
+ * element; element Z owns shell types [EL_SH0[Z], EL_SH0[Z] + EL_NSH[Z]).
+ */
+#define DXTB_MAXZ 87
+#define DXTB_MAXSHT 320
+#define DXTB_MAXPRIM 8
+
+/* float64 table offsets */
+#define DXTB_P_ALPHA 0                                          /* [SHT][8] */
+#define DXTB_P_COEFF (DXTB_P_ALPHA + DXTB_MAXSHT * DXTB_MAXPRIM) /* [SHT][8] */
+#define DXTB_P_LEVEL (DXTB_P_COEFF + DXTB_MAXSHT * DXTB_MAXPRIM) /* Eh      */
+#define DXTB_P_KCN (DXTB_P_LEVEL + DXTB_MAXSHT)                   /* Eh      */
+#define DXTB_P_SHPOLY (DXTB_P_KCN + DXTB_MAXSHT)
+#define DXTB_P_REFOCC (DXTB_P_SHPOLY + DXTB_MAXSHT)
+#define DXTB_P_LGAM (DXTB_P_REFOCC + DXTB_MAXSHT)
+#define DXTB_P_SLATER (DXTB_P_LGAM + DXTB_MAXSHT)
+#define DXTB_P_EN (DXTB_P_SLATER + DXTB_MAXSHT)   /* per element [MAXZ]      */
+#define DXTB_P_GAM (DXTB_P_EN + DXTB_MAXZ)
+#define DXTB_P_GAM3 (DXTB_P_GAM + DXTB_MAXZ)
+#define DXTB_P_ZEFF (DXTB_P_GAM3 + DXTB_MAXZ)
+#define DXTB_P_AREP (DXTB_P_ZEFF + DXTB_MAXZ)
+#define DXTB_P_DKERNEL (DXTB_P_AREP + DXTB_MAXZ)
+#define DXTB_P_QKERNEL (DXTB_P_DKERNEL + DXTB_MAXZ)
+#define DXTB_P_MPRAD (DXTB_P_QKERNEL + DXTB_MAXZ)
+#define DXTB_P_MPVCN (DXTB_P_MPRAD + DXTB_MAXZ)
+#define DXTB_P_RCOV (DXTB_P_MPVCN + DXTB_MAXZ)    /* Bohr, D3 (4/3 scaled)  */
+#define DXTB_P_RAD (DXTB_P_RCOV + DXTB_MAXZ)      /* Bohr, H0 polynomial    */
+#define DXTB_P_VDW (DXTB_P_RAD + DXTB_MAXZ)       /* Bohr, Born radii       */
+#define DXTB_P_KPAIR (DXTB_P_VDW + DXTB_MAXZ)     /* [MAXZ][MAXZ]           */
+#define DXTB_P_KSHELL (DXTB_P_KPAIR + DXTB_MAXZ * DXTB_MAXZ) /* [5][5]      */
+#define DXTB_P_ES3SCALE (DXTB_P_KSHELL + 25)      /* [5] per angular momentum */
+#define DXTB_P_SCAL (DXTB_P_ES3SCALE + 5)         /* scalars, see below     */
+#define DXTB_S_KPOL 0
+#define DXTB_S_WEXP 1
+#define DXTB_S_ENSCALE 2
+#define DXTB_S_GEXP 3
+#define DXTB_S_REP_KEXP 4
+#define DXTB_S_REP_KLIGHT 5   /* < 0: not used (GFN1)                      */
+#define DXTB_S_DMP3 6
+#define DXTB_S_DMP5 7
+#define DXTB_S_MP_KEXP 8
+#define DXTB_S_MP_SHIFT 9
+#define DXTB_S_MP_RMAX 10
+#define DXTB_S_CN_CUTOFF 11
+#define DXTB_S_REP_CUTOFF 12
+#define DXTB_NSCAL 16
+#define DXTB_P_SIZE (DXTB_P_SCAL + DXTB_NSCAL)
+
+/* int32 table offsets */
+#define DXTB_I_L 0                                   /* [SHT] angular momentum */
+#define DXTB_I_NPRIM (DXTB_I_L + DXTB_MAXSHT)        /* [SHT]                  */
+#define DXTB_I_VALENCE (DXTB_I_NPRIM + DXTB_MAXSHT)  /* [SHT] 0/1              */
+#define DXTB_I_ELEM (DXTB_I_VALENCE + DXTB_MAXSHT)   /* [SHT]                  */
+#define DXTB_I_EL_NSH (DXTB_I_ELEM + DXTB_MAXSHT)    /* [MAXZ]                 */
+#define DXTB_I_EL_SH0 (DXTB_I_EL_NSH + DXTB_MAXZ)    /* [MAXZ]                 */
+#define DXTB_I_SCAL (DXTB_I_EL_SH0 + DXTB_MAXZ)
+#define DXTB_IS_METHOD 0      /* 1 = GFN1, 2 = GFN2                         */
+#define DXTB_IS_CN_KIND 1     /* 0 = exp (GFN1), 1 = gfn (GFN2)             */
+#define DXTB_IS_AVERAGE 2     /* 0 harmonic, 1 arithmetic, 2 geometric      */
+#define DXTB_IS_ES3_SHELL 3   /* 1: shell-resolved third order (GFN2)       */
+#define DXTB_IS_MULTIPOLE 4   /* 1: AES2 anisotropic electrostatics (GFN2)  */
+#define DXTB_NISCAL 8
+#define DXTB_I_SIZE (DXTB_I_SCAL + DXTB_NISCAL)
+
+/* ---- packed batch descriptor ------------------------------------------- */
+typedef struct dxtb_batch {
+  int32_t nmol;
+  int32_t max_nao;             /* largest n_m in the batch                  */
+  int32_t max_nat;
+  int32_t max_nsh;
+  const int64_t *atom_off;     /* [nmol+1]                                  */
+  const int64_t *shell_off;    /* [nmol+1]                                  */
+  const int64_t *ao_off;       /* [nmol+1]                                  */
+  const int64_t *mat_off;      /* [nmol+1] prefix of n_m^2                  */
+  const int64_t *nat2_off;     /* [nmol+1] prefix of nat_m^2                */
+  const int64_t *nsh2_off;     /* [nmol+1] prefix of nsh_m^2                */
+  const int64_t *pair_off;     /* [nmol+1] prefix of nsh_m (nsh_m+1) / 2    */
+  const int32_t *numbers;      /* [natoms] atomic numbers                   */
+  const double *positions;     /* [natoms][3] Bohr                          */
+  const int32_t *shell_atom;   /* [nshells] atom index local to molecule    */
+  const int32_t *shell_type;   /* [nshells] global shell type               */
+  const int32_t *shell_ao;     /* [nshells] first AO, local to molecule     */
+  const int32_t *ao_shell;     /* [naos] shell index local to molecule      */
+} dxtb_batch;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* IndexHelper maps, bit-exact with IndexHelper.from_numbers_angular
+ * (basis/indexhelper.py:338-492) for batch_mode 0 (one molecule, nbatch = 1)
+ * and batch mode 1 (nbatch zero-padded rows of nat_max atoms).
+ * dxtb_index_sizes is host-only: numbers_host [nbatch][nat_max], el_nsh_host
+ * [MAXZ] shells per element (0: no parameters), el_ang_host [MAXZ][8] their
+ * angular momenta; sizes_out [4] = (nunique, nushell, nsh_max, nao_max).
+ * dxtb_index_maps fills, on the stream: unique_angular [nushell],
+ * ushells_to_unique [nushell], ushells_per_unique [nunique], unique_out
+ * [nunique] (sorted atomic numbers), and per row: atom_to_unique,
+ * shells_per_atom, shell_index [nat_max]; angular, shells_to_ushell,
+ * shells_to_atom, orbitals_per_shell, orbital_index [nsh_max];
+ * orbitals_to_shell [nao_max]. zmap_scratch: device int64 [3 * MAXZ]. */
+int32_t dxtb_index_sizes(const int64_t *numbers_host, int32_t nbatch,
+                         int32_t nat_max, int32_t batch_mode,
+                         const int32_t *el_nsh_host, const int32_t *el_ang_host,
+                         int64_t *sizes_out);
+int32_t dxtb_index_maps(const int64_t *numbers, int32_t nbatch, int32_t nat_max,
+                        int32_t batch_mode, const int32_t *el_nsh,
+                        const int32_t *el_ang, int64_t nsh_max, int64_t nao_max,
+                        int64_t *unique_angular, int64_t *angular,
+                        int64_t *atom_to_unique, int64_t *ushells_to_unique,
+                        int64_t *ushells_per_unique, int64_t *shells_to_ushell,
+                        int64_t *shells_per_atom, int64_t *shell_index,
+                        int64_t *shells_to_atom, int64_t *orbitals_per_shell,
+                        int64_t *orbital_index, int64_t *orbitals_to_shell,
+                        int64_t *unique_out, int64_t *zmap_scratch, void *stream);
+
+/* Coordination numbers (tad_mctc cn_d3 as called at xtb/gfn1.py:62-64,
+ * xtb/gfn2.py:58-62, coulomb/multipole.py:323-328). kind 0 = exp, 1 = gfn.
+ * cn: [natoms]. */
+int32_t dxtb_coordination_number(const dxtb_batch *b, const double *par_f,
+                                 const int32_t *par_i, int32_t kind, double *cn,
+                                 void *stream);
+
+/* Geometry-only interaction caches: ES2 gamma (coulomb/secondorder.py:
+ * 799-872) [nsh2_off], ES3 Hubbard derivatives (thirdorder.py get_cache)
+ * [nshells], AES2 damping radii and matrices (coulomb/multipole.py:270-448)
+ * mrad [natoms], sd [3][nat2], dd [9][nat2], sq [6][nat2] (component-major
+ * over nat2_off[nmol]; null for GFN1), and the atom-resolved repulsion
+ * energy (classicals/repulsion/base.py:293-348) erep [natoms]. */
+int32_t dxtb_interaction_cache(const dxtb_batch *b, const double *par_f,
+                               const int32_t *par_i, const double *cn_mp,
+                               double *gamma, double *hd, double *mrad,
+                               double *amat_sd, double *amat_dd,
+                               double *amat_sq, double *erep, void *stream);
+
+/* Multipole integrals and core Hamiltonian for every shell pair of the
+ * batch: the PyTorch integral driver (integral/driver/pytorch/impls/
+ * pairs.py:228-399 with kernels/md.py) followed by normalisation, the
+ * r0 -> rj shifts and the traceless transform (integral/container.py:
+ * 182-537) and BaseHamiltonian.build (xtb/base.py:255-372). Outputs:
+ * overlap [mat], h0 [mat] (may be null), dipole [3][mat] and quadrupole
+ * [6][mat] (ket-centred, traceless; null to skip). cn: [natoms] from
+ * dxtb_coordination_number with the method's counting function. */
+int32_t dxtb_multipole_h0(const dxtb_batch *b, const double *par_f,
+                          const int32_t *par_i, const double *cn,
+                          double *overlap, double *h0, double *dipole,
+                          double *quadrupole, void *stream);
+
+/* Raw multipole integrals about the origin as returned by the integral
+ * wrappers overlap/dipint/quadint (integral/wrappers.py:149-315):
+ * overlap [mat], dipole [3][mat], quadrupole [9][mat] (row-major xx..zz),
+ * all normalised, not shifted, not made traceless. */
+int32_t dxtb_multipole_raw(const dxtb_batch *b, const double *par_f,
+                           const int32_t *par_i, double *overlap,
+                           double *dipole, double *quadrupole, void *stream);
+
+/* SCF workspace of one molecule in doubles (n AOs, nat atoms); the caller
+ * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
+int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
+
+/* Self-consistent field for every molecule of the batch in one persistent
+ * launch, one CTA per molecule (scf/iterator.py:51-144 with scf/pure/*,
+ * wavefunction/filling.py:428-742, exlibs/xitorch symeig): Fock build,
+ * generalized eigensolve, Fermi occupations at kT, density, Mulliken
+ * charges and multipole moments, potentials, Anderson mixing of the
+ * potential; per-molecule convergence (max |G(x) - x| < tol) and iteration
+ * cap. order: [nmol] launch order (largest first) or null. Inputs are the
+ * integrals and caches of the calls above, n0 [naos] reference occupation,
+ * nel [nmol][2] alpha/beta electrons, gb_mat [nat2] or null. Outputs:
+ * density [mat], wdensity [mat] (energy-weighted, may be null), coeff [mat]
+ * (orbital j is row j of the block), evals and occ [naos] (unsorted), q
+ * [naos] orbital charges, dp [natoms][3], qp [natoms][6] atomic multipoles,
+ * vorb [naos], vdp [natoms][3], vqp [natoms][6] potentials of the final
+ * charges, energies [nmol][4] = (E_h0 + E_interaction, -TS, iterations,
+ * final residual) and status [nmol]. */
+int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
+                 const double *overlap, const double *h0, const double *dipole,
+                 const double *quadrupole, const double *gamma,
+                 const double *hd, const double *amat_sd, const double *amat_dd,
+                 const double *amat_sq, const double *gb_mat, const double *n0,
+                 const double *nel, double kt, int32_t maxiter, double tol,
+                 const int64_t *ws_off, const int32_t *order,
+                 double *workspace, double *density, double *wdensity,
+                 double *coeff, double *evals, double *occ, double *q,
+                 double *dp, double *qp, double *vorb, double *vdp,
+                 double *vqp, double *energies, int32_t *status, void *stream);
+
+/* Nuclear gradient dE/dR [natoms][3] at the converged SCF (analytic
+ * adjoint; the reference differentiates with autograd through
+ * calculators/types/autograd.py:84-196 and scf/implicit/fixed_point.py).
+ * Accumulates into grad (caller zeroes it). */
+int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
+                      const int32_t *par_i, const double *cn,
+                      const double *cn_mp, const double *mrad,
+                      const double *density, const double *wdensity,
+                      const double *q, const double *dp, const double *qp,
+                      const double *vorb, const double *vdp, const double *vqp,
+                      const double *overlap, const double *dipole,
+                      const double *reserved0, const double *reserved1,
+                      double *dedcn, double *dedcn_mp, double *grad,
+                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DXTB_GB300_H */

@@ -1,0 +1,108 @@
+"""
+Parity of the CUDA path (through the C-ABI library) with the CPU oracle:
+energies within 1e-8 Eh, forces within 1e-6 Eh/Bohr, integrals to 1e-12.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import xtb_oracle as X
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-8   # Eh
+F_TOL = 1e-6   # Eh/Bohr
+G = np.load(__import__("pathlib").Path(__file__).parent / "golden" / "golden.npz")
+OPTS = {"exclude": ["disp", "d4sc", "hal"]}
+
+
+def calc(method, numbers):
+    from dxtb_gb300 import GFN1Calculator, GFN2Calculator
+
+    cls = GFN1Calculator if method == "gfn1" else GFN2Calculator
+    return cls(torch.as_tensor(numbers), opts=OPTS, device="cuda")
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+@pytest.mark.parametrize("name", ["H2", "LiH", "H2O", "CH4", "SiH4", "LYS_xao"])
+def test_energy_forces_fixture_molecules(method, name):
+    num = G[f"{name}/numbers"].astype(np.int64)
+    pos = G[f"{name}/positions"]
+    ref = X.singlepoint(method, num, pos, grad=True, tol=1e-12)
+    c = calc(method, num)
+    p = torch.tensor(pos, device="cuda")
+    e = float(c.get_energy(p))
+    f = c.get_forces(p).cpu().numpy()
+    assert abs(e - ref.energy) < E_TOL
+    assert np.abs(f + ref.extra["gradient"].numpy()).max() < F_TOL
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_batch_of_synthetic_molecules(method):
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.workloads import random_molecule
+
+    mols = [random_molecule(2000 + i, n) for i, n in enumerate([10, 23, 37, 60, 15])]
+    pb = PackedBatch(tables(method), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols])
+    res = run(pb, forces=True)
+    assert (res.status.cpu() == 0).all()
+    g = res.gradient.cpu().numpy()
+    for i, (num, pos) in enumerate(mols):
+        ref = X.singlepoint(method, num, pos, grad=True, tol=1e-12)
+        assert abs(float(res.energy[i]) - ref.energy) < E_TOL
+        gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
+        assert np.abs(gi - ref.extra["gradient"].numpy()).max() < F_TOL
+
+
+def test_multipole_integrals_match_oracle():
+    """S, ket-centred D and traceless Q of a molecule with d shells (SiH4, GFN2)."""
+    from dxtb_gb300 import _lib
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.calculators import tables
+
+    num = G["SiH4/numbers"].astype(np.int64)
+    pos = G["SiH4/positions"]
+    pb = PackedBatch(tables("gfn2"), [num], [torch.tensor(pos)])
+    res = run(pb)
+    n = int(pb.nao[0])
+    S = res.state["S"][: n * n].view(n, n).cpu()
+    D = res.state["D"][: 3 * n * n].view(3, n, n).cpu()
+    Q = res.state["Q"][: 6 * n * n].view(6, n, n).cpu()
+    sysm = X.make_system("gfn2", num)
+    s, d, q = X.integrals(sysm, torch.tensor(pos), 2)
+    assert (S - s).abs().max() < 1e-12
+    assert (D - d).abs().max() < 1e-12
+    assert (Q - q).abs().max() < 1e-12
+
+
+def test_batched_equals_single():
+    from dxtb_gb300.workloads import random_molecule
+
+    mols = [random_molecule(3000 + i, n) for i, n in enumerate([12, 30])]
+    singles = []
+    for num, pos in mols:
+        c = calc("gfn2", num)
+        singles.append(float(c.get_energy(torch.tensor(pos, device="cuda"))))
+    nmax = max(len(m[0]) for m in mols)
+    nums = torch.zeros(2, nmax, dtype=torch.int64)
+    pos = torch.zeros(2, nmax, 3, dtype=torch.float64)
+    for i, (n, p) in enumerate(mols):
+        nums[i, : len(n)] = torch.tensor(n)
+        pos[i, : len(n)] = torch.tensor(p)
+    c = calc("gfn2", nums)
+    e = c.get_energy(pos.cuda()).cpu().numpy()
+    assert np.abs(e - np.array(singles)).max() < 1e-10
+
+
+def test_autograd_backward_uses_adjoint():
+    from dxtb_gb300.workloads import random_molecule
+
+    num, pos = random_molecule(11, 14)
+    c = calc("gfn2", num)
+    p = torch.tensor(pos, device="cuda", requires_grad=True)
+    e = c.get_energy(p)
+    (g,) = torch.autograd.grad(e, p)
+    f = c.get_forces(p)
+    assert torch.allclose(g, -f, atol=1e-12)

@@ -1,0 +1,119 @@
+"""
+The CPU oracle against the fixtures of the reference's own test suite
+(``tests/golden/golden.npz``, extracted by ``tests/golden/make_golden.py``).
+"""
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import xtb_oracle as X
+
+G = np.load(Path(__file__).parent / "golden" / "golden.npz")
+MOLS = ["H2", "LiH", "H2O", "CH4", "SiH4", "LYS_xao"]
+
+
+def mol(name):
+    return G[f"{name}/numbers"].astype(np.int64), G[f"{name}/positions"]
+
+
+@pytest.mark.parametrize("name", MOLS)
+def test_overlap_and_h0_gfn1(name):
+    """test/test_overlap/overlap.npz and test/test_hamiltonian/h0.npz (tblite
+    0.3.0, stored in float32): pins the integrals, H0, the CN and the radii."""
+    num, pos = mol(name)
+    sysm = X.make_system("gfn1", num)
+    p = torch.tensor(pos)
+    s, _, _ = X.integrals(sysm, p, 1)
+    cn = X.coordination_number(num, p, "exp")
+    h = X.hamiltonian(sysm, p, s, cn)
+    assert np.abs(s.numpy() - G[f"{name}/overlap_gfn1"]).max() < 1e-7
+    assert np.abs(h.numpy() - G[f"{name}/h0_gfn1"]).max() < 2e-7
+
+
+def test_planted_radius_error_is_caught(monkeypatch):
+    """A 1 % error in one atomic radius of the oracle breaks the H0 pin."""
+    from dxtb_gb300.data import radii
+
+    bad = radii.ATOMIC_RADII.copy()
+    bad[8] *= 1.01
+    monkeypatch.setattr(radii, "ATOMIC_RADII", bad)
+    num, pos = mol("H2O")
+    sysm = X.make_system("gfn1", num)
+    p = torch.tensor(pos)
+    s, _, _ = X.integrals(sysm, p, 1)
+    h = X.hamiltonian(sysm, p, s, X.coordination_number(num, p, "exp"))
+    assert np.abs(h.numpy() - G["H2O/h0_gfn1"]).max() > 1e-5
+
+
+CLOSED = [2, 4, 10, 12, 18]
+OPEN = [1, 6, 7, 8, 9, 16]
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+@pytest.mark.parametrize("z", CLOSED + OPEN)
+def test_single_atom_scf(method, z):
+    """test/test_scf/test_elements_gfn{1,2}.py reference vector (tblite):
+    E_scf - TS of the free atom. Pins EV2AU, KELVIN2AU, the self-energies,
+    STO-nG, ES2/ES3 on-site terms and the Fermi filling."""
+    ref = G[f"atoms/{method}"][z - 1]
+    r = X.singlepoint(method, [z], np.zeros((1, 3)), tol=1e-13)
+    tol = 1e-9 if z in CLOSED else 2e-8
+    assert abs(r.e_elec + r.e_free - ref) < tol
+
+
+def test_aes2_inline_reference():
+    """test/test_coulomb/test_aes2.py (LiH): AES2 energies and potentials;
+    pins the GFN2 coordination number and the multipole damping."""
+    for func in ("test_energy", "test_potential"):
+        k = lambda n: torch.tensor(G[f"aes2_{func}/{n}"])
+        num = G[f"aes2_{func}/numbers"].astype(np.int64)
+        pos = k("positions")
+        sysm = X.make_system("gfn2", num)
+        a = X.aes2_cache(sysm, pos, X.coordination_number(num, pos, "gfn"))
+        qat, qdp, qqp = k("qat"), k("qdp"), k("qqp")
+        if func == "test_energy":
+            vsd = torch.einsum("ijx,i->jx", a["sd"], qat)
+            vdd = 0.5 * torch.einsum("ijxy,ix->jy", a["dd"], qdp)
+            edp = (a["dk"][:, None] * qdp * qdp).sum(-1) + ((vsd + vdd) * qdp).sum(-1)
+            vqp = torch.einsum("ijx,i->jx", a["sq"], qat)
+            eqp = (a["qk"][:, None] * qqp * X.QSCALE * qqp).sum(-1) + (vqp * qqp).sum(-1)
+            assert torch.allclose(edp, k("ref_eat_dp"), atol=1e-13)
+            assert torch.allclose(eqp, k("ref_eat_qp"), atol=1e-13)
+        else:
+            vat = torch.einsum("ijx,jx->i", a["sd"], qdp) + torch.einsum("ijx,jx->i", a["sq"], qqp)
+            vdp = (torch.einsum("ijx,i->jx", a["sd"], qat) + torch.einsum("ijxy,ix->jy", a["dd"], qdp)
+                   + 2 * a["dk"][:, None] * qdp)
+            vq = torch.einsum("ijx,i->jx", a["sq"], qat) + 2 * a["qk"][:, None] * qqp * X.QSCALE
+            assert torch.allclose(vat, k("ref_vat_mo"), atol=1e-13)
+            assert torch.allclose(vdp, k("ref_vat_dp"), atol=1e-13)
+            assert torch.allclose(vq, k("ref_vat_qp"), atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["H2", "LiH", "H2O", "CH4", "SiH4"])
+def test_gfn1_autograd_forces(name):
+    """test/test_scf/grad.npz '<name>_full': the reference's own autograd
+    gradient of the GFN1 electronic energy (repulsion, dispersion and halogen
+    excluded), stored in float32. Pins the oracle's variational gradient."""
+    num, pos = mol(name)
+    r = X.singlepoint("gfn1", num, pos, grad=True, exclude=("rep",), tol=1e-12)
+    ref = G[f"{name}/grad_elec_gfn1"]
+    assert np.abs(r.extra["gradient"].numpy() - ref).max() < 5e-8
+
+
+def test_oracle_gradient_matches_finite_differences():
+    """The variational gradient (incl. AES2 and repulsion) equals central
+    finite differences of the converged GFN2 energy (step 1e-4 Bohr)."""
+    num, pos = mol("H2O")
+    r = X.singlepoint("gfn2", num, pos, grad=True, tol=1e-13)
+    g = r.extra["gradient"].numpy()
+    h = 1e-4
+    for a, x in [(0, 2), (1, 0), (2, 2)]:
+        pp, pm = pos.copy(), pos.copy()
+        pp[a, x] += h
+        pm[a, x] -= h
+        ep = X.singlepoint("gfn2", num, pp, tol=1e-13).energy
+        em = X.singlepoint("gfn2", num, pm, tol=1e-13).energy
+        assert abs((ep - em) / (2 * h) - g[a, x]) < 1e-7
