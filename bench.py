@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""
+Benchmark: GFN2-xTB energy + forces, molecules/s, on the packed persistent
+GPU path (one launch per stage for the whole batch), with p50/p99 step
+latency, the per-molecule GPU path beside it, and the CPU reference.
+
+Workload: the 256 seeded synthetic molecules of 10-60 atoms (elements
+H/C/N/O/F/S) of the batched GFN2 configuration, energy AND forces (the
+metric is E+F). A step is one single point (SCF + analytic gradient) of
+every molecule of the batch with the inputs resident in HBM.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+N > 1 (torchrun): independent replicas, one batch per rank (weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+import torch
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GFN2 E+F molecules/s batched vs per-molecule at |dE|<1e-8 Eh; p50/p99 ms"
+WORKLOAD = "GFN2 E+F, 256 synthetic molecules of 10-60 atoms (H/C/N/O/F/S), packed batch"
+
+
+def args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--count", type=int, default=256)
+    p.add_argument("--cpu-sample", type=int, default=12, help="molecules timed on the CPU")
+    p.add_argument("--per-molecule", type=int, default=16, help="molecules on the 1-by-1 GPU path")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k]:
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def fp64_peak_tflops(dev) -> float:
+    """Measured FP64 FMA rate of this GPU (TFLOP/s)."""
+    from dxtb_gb300 import _lib
+
+    L = _lib.lib()
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 20000
+    st = _lib.stream_ptr()
+    for _ in range(2):
+        _lib.check(L.dxtb_fp64_fma_probe(iters, blocks, threads, out.data_ptr(), st), "probe")
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(3):
+        s.record()
+        _lib.check(L.dxtb_fp64_fma_probe(iters, blocks, threads, out.data_ptr(), st), "probe")
+        e.record()
+        e.synchronize()
+        best = max(best, 2.0 * 8 * iters * blocks * threads / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def scf_flops(nao: np.ndarray, iters: np.ndarray, forces: bool) -> float:
+    """Algorithmic FP64 work of the SCF launch (per-molecule sum): orthogonaliser
+    (2/3 n^3) + 11.33 n^3 per iteration (basis transform 4n^3, tridiagonalisation
+    4/3 n^3, back-transform 2n^3, C = X C' 2n^3, P = C f C^T 2n^3) + W (2 n^3)."""
+    n3 = nao.astype(np.float64) ** 3
+    return float(((2.0 / 3.0) + iters * (34.0 / 3.0) + (2.0 if forces else 0.0)) @ n3)
+
+
+def cpu_reference(mols, sample: int, method="gfn2"):
+    """The CPU restatement of the reference path (oracle), E + F per molecule."""
+    from oracle import xtb_oracle as X
+
+    threads = torch.get_num_threads()
+    sel = mols[:sample]
+    times, energies = [], []
+    t0 = time.perf_counter()
+    for num, pos in sel:
+        t = time.perf_counter()
+        r = X.singlepoint(method, num, pos, grad=True, tol=1e-10)
+        times.append(time.perf_counter() - t)
+        energies.append(r.energy)
+    total = time.perf_counter() - t0
+    return {
+        "value": len(sel) / total,
+        "unit": "molecules/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"first {len(sel)} of the {len(mols)} molecules, sequential, E+F, float64",
+        "p50_ms": 1e3 * float(np.percentile(times, 50)),
+        "p99_ms": 1e3 * float(np.percentile(times, 99)),
+    }, energies
+
+
+def main():
+    a = args()
+    world, rank, local = dist_setup()
+    from dxtb_gb300.workloads import config_molecules
+
+    mols = config_molecules(2, count=a.count)
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        torch.set_num_threads(os.cpu_count() or 1)
+        vals, lat = [], []
+        cb = None
+        for _ in range(a.warmup if a.warmup < 1 else 1):
+            cpu_reference(mols, 1)
+        for _ in range(a.steps):
+            cb, _ = cpu_reference(mols, a.cpu_sample)
+            vals.append(cb["value"])
+        v = float(np.median(vals))
+        cb["value"] = v
+        line = {
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "molecules/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * a.cpu_sample / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "molecules/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    from dxtb_gb300 import GFN2Calculator
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+
+    nums = [m[0] for m in mols]
+    pos = [torch.tensor(m[1]) for m in mols]
+    pb = PackedBatch(tables("gfn2"), nums, pos, dev)
+    state: dict = {}
+    l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    for _ in range(a.warmup):
+        res = run(pb, forces=True, state=state)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = Clocks(local)
+    step_ev, stage_ev = [], []
+    for k in range(a.steps):
+        l2.fill_(float(k))  # flush L2 between timed steps
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        evs: dict = {}
+        s.record()
+        res = run(pb, forces=True, state=state, events=evs)
+        e.record()
+        step_ev.append((s, e))
+        stage_ev.append(evs)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in step_ev]
+    total_s = max_over_ranks(sum(step_ms) * 1e-3, world)
+    stages = {
+        k: float(np.mean([ev[k][0].elapsed_time(ev[k][1]) for ev in stage_ev]))
+        for k in stage_ev[0]
+    }
+    status = res.status.cpu().numpy()
+    iters = res.iterations.cpu().numpy()
+    value = pb.nmol * a.steps * world / total_s
+
+    # roofline of the dominant kernel (the persistent SCF launch)
+    peak = fp64_peak_tflops(dev)
+    flops = scf_flops(pb.nao, iters, True)
+    achieved = flops / (stages["scf"] * 1e-3) / 1e12
+
+    # per-molecule GPU path (same kernels, one molecule per launch)
+    per = []
+    for i in range(min(a.per_molecule, pb.nmol)):
+        pbi = PackedBatch(tables("gfn2"), [nums[i]], [pos[i]], dev)
+        sti: dict = {}
+        run(pbi, forces=True, state=sti)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        run(pbi, forces=True, state=sti)
+        e.record()
+        e.synchronize()
+        per.append(s.elapsed_time(e))
+    per_mol_value = len(per) / (sum(per) * 1e-3)
+
+    # end to end through the public API: pinned host positions in, E and F out
+    e2e = None
+    if not a.no_e2e:
+        nmax = max(len(n) for n in nums)
+        znum = torch.zeros(len(nums), nmax, dtype=torch.int64)
+        hpos = torch.zeros(len(nums), nmax, 3, dtype=torch.float64).pin_memory()
+        for i, (n, p) in enumerate(zip(nums, pos)):
+            znum[i, : len(n)] = torch.as_tensor(n)
+            hpos[i, : len(n)] = p
+        calc = GFN2Calculator(znum, opts={"exclude": ["disp", "d4sc"]}, device=dev)
+        for _ in range(a.warmup):
+            dpos = hpos.to(dev, non_blocking=True)
+            f = calc.get_forces(dpos)
+            en = calc.get_energy(dpos)
+        torch.cuda.synchronize()
+        t_e2e = []
+        h_e = torch.empty(len(nums), dtype=torch.float64).pin_memory()
+        h_f = torch.empty_like(hpos).pin_memory()
+        for k in range(a.steps):
+            l2.fill_(float(k))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dpos = hpos.to(dev, non_blocking=True)
+            f = calc.get_forces(dpos)
+            en = calc.get_energy(dpos)
+            h_f.copy_(f)
+            h_e.copy_(en)
+            t_e2e.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(sum(t_e2e), world)
+        e2e = {
+            "value": len(nums) * a.steps * world / e2e_s,
+            "unit": "molecules/s",
+            "h2d_bytes_per_step": int(hpos.numel() * 8),
+            "d2h_bytes_per_step": int(h_f.numel() * 8 + h_e.numel() * 8),
+            "p50_ms": 1e3 * float(np.percentile(t_e2e, 50)),
+            "p99_ms": 1e3 * float(np.percentile(t_e2e, 99)),
+        }
+
+    cpu_baseline = None
+    max_de = None
+    if rank == 0 and a.cpu_sample > 0:
+        cpu_baseline, ref_e = cpu_reference(mols, a.cpu_sample)
+        got = res.energy.cpu().numpy()[: len(ref_e)]
+        max_de = float(np.abs(got - np.array(ref_e)).max())
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "molecules/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": float(np.mean(step_ms)),
+        "p50_ms": float(np.percentile(step_ms, 50)),
+        "p99_ms": float(np.percentile(step_ms, 99)),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD,
+            "molecules": pb.nmol,
+            "atoms": int(pb.atom_off[-1]),
+            "aos_total": int(pb.ao_off[-1]),
+            "nao_min_max": [int(pb.nao.min()), int(pb.nao.max())],
+            "l2": "flushed between timed steps (256 MB write)",
+            "parallelism": f"replicas x{world}",
+            "scf_iterations_mean_max": [float(iters.mean()), float(iters.max())],
+            "status_ok": int((status == 0).sum()),
+        },
+        "stages_ms": stages,
+        "per_molecule": {"value": per_mol_value, "unit": "molecules/s", "molecules": len(per),
+                         "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99))},
+        "speedup_vs_per_molecule": value / per_mol_value,
+        "parity": {"max_abs_dE_vs_cpu_reference_sample": max_de},
+        "roofline": {
+            "kernel": "k_scf (persistent SCF, one CTA per molecule)",
+            "bound": "fp64",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / peak,
+            "peak_source": "measured FP64 FMA probe (dxtb_fp64_fma_probe) on this GPU",
+            "traffic": None,
+        },
+        "cpu_baseline": cpu_baseline,
+        "e2e": e2e,
+        "gpu_launches": 6 * a.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

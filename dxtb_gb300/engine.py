@@ -181,9 +181,23 @@ def _seg_sum(values: torch.Tensor, off: np.ndarray, nmol: int) -> torch.Tensor:
 
 
 def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float = 1e-10,
-        forces: bool = False, gb: dict | None = None, state: dict | None = None) -> Result:
-    """One single point for every molecule of the packed batch."""
+        forces: bool = False, gb: dict | None = None, state: dict | None = None,
+        events: dict | None = None) -> Result:
+    """
+    One single point for every molecule of the packed batch. With ``events``
+    (a dict), CUDA events are recorded on the current stream around each
+    stage: events[stage] = (start, end).
+    """
     L = _lib.lib()
+
+    def mark(stage, which):
+        if events is not None:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            if which == 0:
+                events[stage] = [ev, None]
+            else:
+                events[stage][1] = ev
     from .data import radii
 
     tb = pb.tables
@@ -204,6 +218,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
     na, ns, no, nm, n2, g2 = tot["atoms"], tot["shells"], tot["aos"], tot["mat"], tot["nat2"], tot["nsh2"]
     mp = tb.multipole
     cn = buf("cn", na)
+    mark("geometry", 0)
     _lib.check(L.dxtb_coordination_number(b, pf, pi, tb.cn_kind, cn.data_ptr(), st), "coordination number")
     cn_mp = cn
     if mp and tb.cn_kind != 1:
@@ -234,8 +249,11 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
     S, H = buf("S", nm), buf("H", nm)
     D = buf("D", 3 * nm) if mp else None
     Q = buf("Q", 6 * nm) if mp else None
+    mark("geometry", 1)
+    mark("integrals", 0)
     _lib.check(L.dxtb_multipole_h0(b, pf, pi, cn.data_ptr(), S.data_ptr(), H.data_ptr(),
                                    _lib.ptr(D), _lib.ptr(Q), st), "multipole integrals")
+    mark("integrals", 1)
     P, Cm = buf("P", nm), buf("C", nm)
     W = buf("W", nm) if forces else None
     ev, occ, q = buf("evals", no), buf("occ", no), buf("q", no)
@@ -249,6 +267,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
         s["status"] = status
     ws = buf("ws", tot["ws"])
     kt = etemp * radii.KELVIN2AU
+    mark("scf", 0)
     _lib.check(
         L.dxtb_scf(b, pf, pi, S.data_ptr(), H.data_ptr(), _lib.ptr(D), _lib.ptr(Q), gamma.data_ptr(),
                    hd.data_ptr(), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq), _lib.ptr(gbm),
@@ -259,6 +278,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                    en.data_ptr(), status.data_ptr(), st),
         "SCF",
     )
+    mark("scf", 1)
     e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
     e_rep = _seg_sum(erep[:na], pb.atom_off, pb.nmol)
     grad = None
@@ -270,6 +290,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
         dedcn.zero_()
         if dedcn_mp is not None:
             dedcn_mp.zero_()
+        mark("gradient", 0)
         _lib.check(
             L.dxtb_gradient(b, pf, pi, cn.data_ptr(), cn_mp.data_ptr(), _lib.ptr(mrad), P.data_ptr(),
                             W.data_ptr(), q.data_ptr(), dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(),
@@ -277,6 +298,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                             dedcn.data_ptr(), _lib.ptr(dedcn_mp), grad.data_ptr(), st),
             "gradient",
         )
+        mark("gradient", 1)
         if gb is not None:
             _lib.check(
                 L.dxtb_born_gradient(b, pf, pi, q.data_ptr(), s["born"].data_ptr(), s["psi"].data_ptr(),

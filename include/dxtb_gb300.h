@@ -240,6 +240,12 @@ int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
                       double *dedcn, double *dedcn_mp, double *grad,
                       void *stream);
 
+/* FP64 FMA throughput probe used as the measured FP64 roofline denominator:
+ * blocks x threads threads each run 8 independent FMA chains of iters
+ * steps (2 * 8 * iters flops per thread). No counterpart in the reference. */
+int32_t dxtb_fp64_fma_probe(int64_t iters, int32_t blocks, int32_t threads,
+                            double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
