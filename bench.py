@@ -108,7 +108,7 @@ class Clocks:
             except (ValueError, IndexError):
                 continue
             for k, name in enumerate(names):
-                if len(r) > 5 + k and "Active" in r[5 + k]:
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
                     reasons.add(name)
         return {
             "sm_mhz": statistics.median(sm) if sm else None,
@@ -283,6 +283,7 @@ def main():
         h_f = torch.empty_like(hpos).pin_memory()
         for k in range(a.steps):
             l2.fill_(float(k))
+            calc.reset()  # no result reuse across steps: every step computes
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             dpos = hpos.to(dev, non_blocking=True)
