@@ -565,3 +565,92 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   DXTB_CHECK_LAUNCH();
   return DXTB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// SCF entry point for callers that cannot allocate device memory.
+//
+// Some callers cannot call cudaMalloc at all: code that runs while a CUDA
+// graph is being captured by someone else, hosts that hand the library a
+// fixed memory pool and forbid further device allocations, or plugin hosts
+// whose allocator is not reachable from the C ABI. dxtb_scf_noalloc serves
+// them: it runs the same persistent SCF kernel as dxtb_scf, but its scratch
+// workspace is a fixed array in the library's own device memory, so the
+// caller passes only the inputs and the output buffers.
+//
+// The array holds DXTB_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) and every
+// GPU that loads the library keeps it until the process exits. Batches whose
+// workspace does not fit are rejected with DXTB_ERR_TOO_LARGE.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace dxtb {
+
+static __device__ __align__(256) double g_scf_scratch[DXTB_NOALLOC_SCRATCH_DOUBLES];
+
+// Header of the scratch array: [0] required doubles (int64), [1 .. nmol+1]
+// per-molecule workspace offsets (int64, relative to the workspace start).
+constexpr int64_t kNoallocHeader = 1;
+
+__global__ void k_noalloc_layout(dxtb_batch b, int64_t *hdr, int64_t ws_start) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t off = 0;
+  for (int m = 0; m < b.nmol; ++m) {
+    hdr[kNoallocHeader + m] = off;
+    const int64_t n = b.ao_off[m + 1] - b.ao_off[m];
+    const int64_t nat = b.atom_off[m + 1] - b.atom_off[m];
+    off += ws_size_mol(n, nat);
+  }
+  hdr[kNoallocHeader + b.nmol] = off;
+  hdr[0] = ws_start + off;  // doubles needed from the start of the array
+}
+
+static std::mutex g_noalloc_mutex;
+static double *g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array for the current device, looked up
+// once per device (host code must not use the symbol itself as a pointer).
+static int32_t noalloc_scratch(double **out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scf_scratch) != cudaSuccess || p == nullptr)
+      return DXTB_ERR_LAUNCH;
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return DXTB_OK;
+}
+
+}  // namespace dxtb
+
+extern "C" int32_t dxtb_scf_noalloc(
+    const dxtb_batch *b, const double *par_f, const int32_t *par_i, const double *overlap,
+    const double *h0, const double *dipole, const double *quadrupole, const double *gamma,
+    const double *hd, const double *amat_sd, const double *amat_dd, const double *amat_sq,
+    const double *gb_mat, const double *n0, const double *nel, double kt, int32_t maxiter,
+    double tol, const int32_t *order, double *density, double *wdensity, double *coeff,
+    double *evals, double *occ, double *q, double *dp, double *qp, double *vorb, double *vdp,
+    double *vqp, double *energies, int32_t *status, void *stream) {
+  if (!b || b->nmol <= 0) return DXTB_ERR_ARGS;
+  // header (nmol + 2 int64) must fit before the workspace
+  const int64_t ws_start = ((kNoallocHeader + b->nmol + 1) + 31) / 32 * 32;
+  if (ws_start >= DXTB_NOALLOC_SCRATCH_DOUBLES) return DXTB_ERR_TOO_LARGE;
+  double *scratch = nullptr;
+  int32_t rc = noalloc_scratch(&scratch);
+  if (rc != DXTB_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t *hdr = reinterpret_cast<int64_t *>(scratch);
+  k_noalloc_layout<<<1, 32, 0, st>>>(*b, hdr, ws_start);
+  DXTB_CHECK_LAUNCH();
+  int64_t need = 0;
+  if (cudaMemcpyAsync(&need, hdr, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return DXTB_ERR_LAUNCH;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (need > DXTB_NOALLOC_SCRATCH_DOUBLES) return DXTB_ERR_TOO_LARGE;
+  return dxtb_scf(b, par_f, par_i, overlap, h0, dipole, quadrupole, gamma, hd, amat_sd, amat_dd,
+                  amat_sq, gb_mat, n0, nel, kt, maxiter, tol, hdr + kNoallocHeader, order,
+                  scratch + ws_start, density, wdensity, coeff, evals, occ, q, dp, qp, vorb, vdp,
+                  vqp, energies, status, stream);
+}

@@ -240,6 +240,37 @@ int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
                       double *dedcn, double *dedcn_mp, double *grad,
                       void *stream);
 
+/* SCF without any device allocation. No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (code running under someone
+ * else's stream capture, hosts that forbid allocations outside a fixed
+ * pool, plugin hosts without access to an allocator). It runs the kernel of
+ * dxtb_scf with the same inputs and outputs, but takes its scratch
+ * workspace from a fixed array inside the library (DXTB_NOALLOC_SCRATCH_
+ * DOUBLES doubles = 16 MiB per GPU that loads the library, held until the
+ * process exits) instead of caller memory. A batch whose workspace
+ * (sum over molecules of dxtb_scf_workspace_mol plus nmol + 2 header words)
+ * does not fit returns DXTB_ERR_TOO_LARGE without running.
+ * The first call on a device looks up the array's device address (set-up);
+ * make that first call before any stream capture. All calls share the one
+ * array, which keeps the last call's contents (nothing in it needs to start
+ * at zero): calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. The call synchronises the
+ * stream once to check the size. */
+#define DXTB_NOALLOC_SCRATCH_DOUBLES (1 << 21)
+int32_t dxtb_scf_noalloc(const dxtb_batch *b, const double *par_f,
+                         const int32_t *par_i, const double *overlap,
+                         const double *h0, const double *dipole,
+                         const double *quadrupole, const double *gamma,
+                         const double *hd, const double *amat_sd,
+                         const double *amat_dd, const double *amat_sq,
+                         const double *gb_mat, const double *n0,
+                         const double *nel, double kt, int32_t maxiter,
+                         double tol, const int32_t *order, double *density,
+                         double *wdensity, double *coeff, double *evals,
+                         double *occ, double *q, double *dp, double *qp,
+                         double *vorb, double *vdp, double *vqp,
+                         double *energies, int32_t *status, void *stream);
+
 /* FP64 FMA throughput probe used as the measured FP64 roofline denominator:
  * blocks x threads threads each run 8 independent FMA chains of iters
  * steps (2 * 8 * iters flops per thread). No counterpart in the reference. */
