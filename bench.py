@@ -261,7 +261,7 @@ def main():
         e.record()
         e.synchronize()
         per.append(s.elapsed_time(e))
-    per_mol_value = len(per) / (sum(per) * 1e-3)
+    per_mol_value = len(per) / (sum(per) * 1e-3) if per else None
 
     # end to end through the public API: pinned host positions in, E and F out
     e2e = None
@@ -338,8 +338,9 @@ def main():
         },
         "stages_ms": stages,
         "per_molecule": {"value": per_mol_value, "unit": "molecules/s", "molecules": len(per),
-                         "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99))},
-        "speedup_vs_per_molecule": value / per_mol_value,
+                         "p50_ms": float(np.percentile(per, 50)) if per else None,
+                         "p99_ms": float(np.percentile(per, 99)) if per else None},
+        "speedup_vs_per_molecule": value / per_mol_value if per_mol_value else None,
         "parity": {"max_abs_dE_vs_cpu_reference_sample": max_de},
         "roofline": {
             "kernel": "k_scf (persistent SCF, one CTA per molecule)",

@@ -1,22 +1,42 @@
 // CTA-level dense float64 linear algebra for one molecule's AO matrices
 // (row-major, leading dimension n, resident in global memory / L2). Every
 // routine must be called by all threads of the block.
+//
+// The symmetric eigenproblem of the SCF is solved as
+//   Householder tridiagonalisation  (cta_tridiag)
+//   -> eigenvalues by implicit QL without vectors (cta_tql_values)
+//   -> eigenvectors of the lowest m eigenvalues only, by inverse iteration
+//      with a pivoted tridiagonal LU, one thread per eigenvalue cluster,
+//      Gram-Schmidt inside clusters (cta_tri_vectors)
+//   -> back-transformation of those m vectors (cta_back_transform).
+// The SCF needs only the orbitals with non-vanishing occupation, so the
+// O(n^3) accumulation of QL rotations is never done.
 #pragma once
 #include "common.cuh"
 
 namespace dxtb {
 
+// Shapes of the k-loop for triangular operands.
+enum KRange : int {
+  kFull = 0,     // k in [0, K)
+  kALower = 1,   // op(A)(i,k) = 0 for k > i   -> k < i0 + 4
+  kBLowerT = 2,  // op(B)(k,j) = 0 for k > j   -> k < j0 + 4
+  kBUpper = 3,   // op(B)(k,j) = 0 for k < j   -> k >= j0
+};
+
 // C = alpha * op(A) op(B) + beta * C for M x N outputs and inner size K.
 // op(A)(i,k) = TA ? A[k*lda+i] : A[i*lda+k]; op(B)(k,j) = TB ? B[j*ldb+k] : B[k*ldb+j].
-// Register tile of 4 x 4 outputs per thread; the FP64 pipe, not memory, is
-// the limit at these sizes.
+// Register tile of 4 x 4 outputs per thread. With lower_only, tiles strictly
+// above the diagonal are skipped (symmetric results). The FP64 pipe, not
+// memory, is the limit at these sizes.
 template <bool TA, bool TB>
-__device__ void cta_gemm(int M, int N, int K, double alpha, const double *__restrict__ A,
-                         int lda, const double *__restrict__ B, int ldb, double beta,
-                         double *__restrict__ C, int ldc) {
+__device__ void cta_gemm(int M, int N, int K, double alpha, const double *__restrict__ A, int lda,
+                         const double *__restrict__ B, int ldb, double beta, double *__restrict__ C,
+                         int ldc, int krange = kFull, bool lower_only = false) {
   const int tm = (M + 3) >> 2, tn = (N + 3) >> 2;
   for (int t = threadIdx.x; t < tm * tn; t += blockDim.x) {
     const int i0 = (t / tn) * 4, j0 = (t % tn) * 4;
+    if (lower_only && j0 > i0 + 3) continue;
     double acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -28,7 +48,11 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *__rest
       ia[a] = min(i0 + a, M - 1);
       jb[a] = min(j0 + a, N - 1);
     }
-    for (int k = 0; k < K; ++k) {
+    int k0 = 0, k1 = K;
+    if (krange == kALower) k1 = min(K, i0 + 4);
+    else if (krange == kBLowerT) k1 = min(K, j0 + 4);
+    else if (krange == kBUpper) k0 = j0;
+    for (int k = k0; k < k1; ++k) {
       double av[4], bv[4];
 #pragma unroll
       for (int a = 0; a < 4; ++a) av[a] = TA ? A[(size_t)k * lda + ia[a]] : A[(size_t)ia[a] * lda + k];
@@ -44,7 +68,7 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *__rest
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const int i = i0 + a, j = j0 + c;
-        if (i < M && j < N) {
+        if (i < M && j < N && (!lower_only || j <= i)) {
           double *p = C + (size_t)i * ldc + j;
           *p = alpha * acc[a][c] + (beta == 0.0 ? 0.0 : beta * *p);
         }
@@ -53,9 +77,18 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *__rest
   __syncthreads();
 }
 
+// Copy the lower triangle of a square matrix onto its upper triangle.
+__device__ void cta_mirror_lower(int n, double *A) {
+  for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (j > i) A[t] = A[(size_t)j * n + i];
+  }
+  __syncthreads();
+}
+
 // In-place lower Cholesky factor of a symmetric positive-definite matrix
 // (right-looking). Returns false if a pivot is not positive.
-__device__ bool cta_cholesky(int n, double *A, double *red) {
+__device__ bool cta_cholesky(int n, double *A) {
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
   __syncthreads();
@@ -77,7 +110,6 @@ __device__ bool cta_cholesky(int n, double *A, double *red) {
     }
     __syncthreads();
   }
-  (void)red;
   return true;
 }
 
@@ -164,119 +196,219 @@ __device__ void cta_tridiag(int n, double *A, double *d, double *e, double *tau,
   __syncthreads();
 }
 
-// Q = H_0 H_1 ... H_{n-3} from the reflectors of cta_tridiag, written
-// transposed: Zt[j][r] = Q[r][j] (column j of Q is row j of Zt).
-// Backward accumulation on row-major scratch Qs, then transpose.
-__device__ void cta_form_q(int n, const double *A, const double *tau, double *Qs, double *Zt,
-                           double *w) {
-  for (int64_t q = threadIdx.x; q < (int64_t)n * n; q += blockDim.x)
-    Qs[q] = (q / n == q % n) ? 1.0 : 0.0;
-  __syncthreads();
-  for (int k = n - 3; k >= 0; --k) {
-    const double t = tau[k];
-    if (t == 0.0) continue;
-    const int m = n - k - 1;
-    const double *col = A + (size_t)(k + 1) * n + k;
-    double *Qb = Qs + (size_t)(k + 1) * n + (k + 1);
-    for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      double s = Qb[c];
-      for (int r = 1; r < m; ++r) s = fma(col[(size_t)r * n], Qb[(size_t)r * n + c], s);
-      w[c] = t * s;
-    }
-    __syncthreads();
-    for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) {
-      const int r = (int)(q / m), c = (int)(q % m);
-      const double vr = r == 0 ? 1.0 : col[(size_t)r * n];
-      Qb[(size_t)r * n + c] -= vr * w[c];
-    }
-    __syncthreads();
+// Eigenvalues of the symmetric tridiagonal (d, e) by implicit QL with
+// Wilkinson-type shifts (Bowdler, Martin, Reinsch, Wilkinson, Numer. Math.
+// 11, 293 (1968)), without eigenvector accumulation. Thread 0 runs the
+// scalar recurrence on the scratch copies sd, se (shared memory when they
+// fit); lam receives the (unsorted) eigenvalues. False if an eigenvalue
+// needs more than 60 sweeps.
+__device__ bool cta_tql_values(int n, const double *d, const double *e, double *sd, double *se,
+                               double *lam) {
+  __shared__ int s_ok;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    sd[i] = d[i];
+    se[i] = e[i];
   }
-  for (int64_t q = threadIdx.x; q < (int64_t)n * n; q += blockDim.x) {
-    const int r = (int)(q / n), c = (int)(q % n);
-    Zt[(size_t)c * n + r] = Qs[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    for (int l = 0; l < n && ok; ++l) {
+      int iter = 0;
+      while (true) {
+        int m = l;
+        for (; m < n - 1; ++m) {
+          const double dd = fabs(sd[m]) + fabs(sd[m + 1]);
+          if (fabs(se[m]) <= kEps * dd) break;
+        }
+        if (m == l) break;
+        if (++iter > 60) {
+          ok = 0;
+          break;
+        }
+        double g = (sd[l + 1] - sd[l]) / (2.0 * se[l]);
+        double r = sqrt(g * g + 1.0);
+        g = sd[m] - sd[l] + se[l] / (g + copysign(r, g));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i = m - 1;
+        bool early = false;
+        for (; i >= l; --i) {
+          const double f = s * se[i], bb = c * se[i];
+          r = sqrt(f * f + g * g);
+          se[i + 1] = r;
+          if (r == 0.0) {
+            sd[i + 1] -= p;
+            se[m] = 0.0;
+            early = true;
+            break;
+          }
+          const double ir = 1.0 / r;
+          s = f * ir;
+          c = g * ir;
+          g = sd[i + 1] - p;
+          r = (sd[i] - g) * s + 2.0 * c * bb;
+          p = s * r;
+          sd[i + 1] = g + p;
+          g = c * r - bb;
+        }
+        if (!early) {
+          sd[l] -= p;
+          se[l] = g;
+          se[m] = 0.0;
+        }
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sd[i];
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Ascending sort by rank (ties broken by index): out[rank(i)] = in[i].
+__device__ void cta_rank_sort(int n, const double *in, double *out) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = in[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const double u = in[j];
+      r += (u < v) || (u == v && j < i);
+    }
+    out[r] = v;
   }
   __syncthreads();
 }
 
-// Implicit QL with Wilkinson-type shifts on the tridiagonal (d, e) of order
-// n (Bowdler, Martin, Reinsch, Wilkinson, Numer. Math. 11, 293 (1968)),
-// applying the plane rotations to the eigenvector rows Zt (Zt[j][:] is
-// vector j). Thread 0 runs the scalar recurrence of one sweep and records
-// the rotations; then all threads apply them, each to its own components.
-// Returns false if an eigenvalue needs more than 60 sweeps.
-__device__ bool cta_tql(int n, double *d, double *e, double *Zt, double *rc, double *rs) {
-  __shared__ int s_m, s_lo, s_state;  // state: 0 converged l, 1 rotate, 2 fail
-  for (int l = 0; l < n; ++l) {
-    int iter = 0;
-    while (true) {
-      if (threadIdx.x == 0) {
-        int m = l;
-        for (; m < n - 1; ++m) {
-          const double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= kEps * dd) break;
-        }
-        if (m == l) {
-          s_state = 0;
-        } else if (++iter > 60) {
-          s_state = 2;
+__device__ __forceinline__ double start_vector(int i, int j) {
+  // deterministic pseudo-random start in [0.5, 1.5) (any vector with a
+  // component along the eigenvector works)
+  uint32_t h = 2654435761u * (uint32_t)(i + 1) ^ 40503u * (uint32_t)(j + 7);
+  h ^= h >> 13;
+  h *= 0x5bd1e995u;
+  h ^= h >> 15;
+  return 0.5 + (double)(h & 0xffffff) / 16777216.0;
+}
+
+// Eigenvectors of the symmetric tridiagonal (d, e) for the m lowest
+// (sorted) eigenvalues lam[0..m) by inverse iteration with a partially
+// pivoted LU of T - lam I (the scheme of LAPACK's dstein: three solves,
+// re-orthogonalisation against the previous members of the cluster).
+// Clusters are runs of eigenvalues closer than ctol; each cluster is one
+// thread's work. Y: n x m row-major (column j = vector j).
+// lu: scratch of 5 * n * blockDim doubles. cl: int scratch of m + 1.
+__device__ void cta_tri_vectors(int n, const double *d, const double *e, const double *lam, int m,
+                                double tnorm, double *Y, double *lu, int *cl, int *s_ncl) {
+  const double ctol = 1e-6 * fmax(tnorm, 1.0);
+  const double tiny = kEps * fmax(tnorm, 1.0);
+  if (threadIdx.x == 0) {
+    int c = 0;
+    cl[c++] = 0;
+    for (int j = 1; j < m; ++j)
+      if (lam[j] - lam[j - 1] > ctol) cl[c++] = j;
+    cl[c] = m;
+    *s_ncl = c;
+  }
+  __syncthreads();
+  const int ncl = *s_ncl;
+  const int nthr = blockDim.x, tid = threadIdx.x;
+  double *U0 = lu, *U1 = lu + (size_t)n * nthr, *U2 = lu + 2 * (size_t)n * nthr;
+  double *Lm = lu + 3 * (size_t)n * nthr, *Pv = lu + 4 * (size_t)n * nthr;
+#define LU(arr, i) arr[(size_t)(i) * nthr + tid]
+  for (int c = tid; c < ncl; c += nthr) {
+    const int j0 = cl[c], j1 = cl[c + 1];
+    for (int j = j0; j < j1; ++j) {
+      // separate exactly coincident shifts inside a cluster (dstein)
+      const double lmb = lam[j] + (j - j0) * 10.0 * tiny;
+      // LU with partial pivoting of T - lmb I; rows hold (diag, super, super2)
+      double a = d[0] - lmb, bsup = n > 1 ? e[0] : 0.0;
+      for (int i = 0; i < n - 1; ++i) {
+        const double low = e[i];
+        const double dn = d[i + 1] - lmb, en = (i + 1 < n - 1) ? e[i + 1] : 0.0;
+        if (fabs(a) >= fabs(low)) {
+          const double piv = a == 0.0 ? tiny : a;
+          const double mult = low / piv;
+          LU(U0, i) = piv;
+          LU(U1, i) = bsup;
+          LU(U2, i) = 0.0;
+          LU(Lm, i) = mult;
+          LU(Pv, i) = 0.0;
+          a = dn - mult * bsup;
+          bsup = en;
         } else {
-          double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-          double r = hypot(g, 1.0);
-          g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-          double s = 1.0, c = 1.0, p = 0.0;
-          int i = m - 1;
-          bool early = false;
-          for (; i >= l; --i) {
-            const double f = s * e[i], bb = c * e[i];
-            r = hypot(f, g);
-            e[i + 1] = r;
-            if (r == 0.0) {
-              d[i + 1] -= p;
-              e[m] = 0.0;
-              early = true;
-              break;
-            }
-            s = f / r;
-            c = g / r;
-            g = d[i + 1] - p;
-            r = (d[i] - g) * s + 2.0 * c * bb;
-            p = s * r;
-            d[i + 1] = g + p;
-            g = c * r - bb;
-            rc[i] = c;
-            rs[i] = s;
-          }
-          if (!early) {
-            d[l] -= p;
-            e[l] = g;
-            e[m] = 0.0;
-          }
-          s_m = m;
-          s_lo = early ? i + 1 : l;  // rotations recorded for [s_lo, m-1]
-          s_state = 1;
+          const double mult = a / low;
+          LU(U0, i) = low;
+          LU(U1, i) = dn;
+          LU(U2, i) = en;
+          LU(Lm, i) = mult;
+          LU(Pv, i) = 1.0;
+          a = bsup - mult * dn;
+          bsup = -mult * en;
         }
       }
-      __syncthreads();
-      const int state = s_state;
-      if (state == 2) return false;
-      if (state == 0) break;
-      const int m = s_m, lo = s_lo;
-      if (lo <= m - 1) {
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-          double cur = Zt[(size_t)m * n + k];
-          for (int i = m - 1; i >= lo; --i) {
-            const double zi = Zt[(size_t)i * n + k];
-            const double c = rc[i], s = rs[i];
-            Zt[(size_t)(i + 1) * n + k] = s * zi + c * cur;
-            cur = c * zi - s * cur;
+      LU(U0, n - 1) = fabs(a) < tiny ? copysign(tiny, a == 0.0 ? 1.0 : a) : a;
+      for (int i = 0; i < n - 1; ++i)
+        if (fabs(LU(U0, i)) < tiny) LU(U0, i) = copysign(tiny, LU(U0, i) == 0.0 ? 1.0 : LU(U0, i));
+      for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
+      for (int it = 0; it < 3; ++it) {
+        // forward: apply the row interchanges and multipliers
+        for (int i = 0; i < n - 1; ++i) {
+          double xi = Y[(size_t)i * m + j], xn = Y[(size_t)(i + 1) * m + j];
+          if (LU(Pv, i) != 0.0) {
+            const double t = xi;
+            xi = xn;
+            xn = t;
           }
-          Zt[(size_t)lo * n + k] = cur;
+          Y[(size_t)i * m + j] = xi;
+          Y[(size_t)(i + 1) * m + j] = xn - LU(Lm, i) * xi;
         }
+        // back substitution with the upper factor (two super-diagonals)
+        double x1 = 0.0, x2 = 0.0;
+        for (int i = n - 1; i >= 0; --i) {
+          const double v = (Y[(size_t)i * m + j] - LU(U1, i) * x1 - LU(U2, i) * x2) / LU(U0, i);
+          Y[(size_t)i * m + j] = v;
+          x2 = x1;
+          x1 = v;
+        }
+        // Gram-Schmidt against the earlier members of the cluster
+        for (int k = j0; k < j; ++k) {
+          double dot = 0.0;
+          for (int i = 0; i < n; ++i) dot += Y[(size_t)i * m + k] * Y[(size_t)i * m + j];
+          for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] -= dot * Y[(size_t)i * m + k];
+        }
+        double nrm = 0.0;
+        for (int i = 0; i < n; ++i) nrm += Y[(size_t)i * m + j] * Y[(size_t)i * m + j];
+        const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
+        for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
       }
-      __syncthreads();
     }
   }
-  return true;
+#undef LU
+  __syncthreads();
+}
+
+// Y <- Q Y for the reflectors stored by cta_tridiag (Q = H_0 ... H_{n-3});
+// Y is n x m row-major. w: scratch of m doubles.
+__device__ void cta_back_transform(int n, const double *A, const double *tau, double *Y, int m,
+                                   double *w) {
+  for (int k = n - 3; k >= 0; --k) {
+    const double t = tau[k];
+    if (t == 0.0) continue;
+    const int mm = n - k - 1;
+    const double *col = A + (size_t)(k + 1) * n + k;
+    double *Yb = Y + (size_t)(k + 1) * m;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      double s = Yb[j];
+      for (int r = 1; r < mm; ++r) s = fma(col[(size_t)r * n], Yb[(size_t)r * m + j], s);
+      w[j] = t * s;
+    }
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < (int64_t)mm * m; q += blockDim.x) {
+      const int r = (int)(q / m), j = (int)(q % m);
+      const double vr = r == 0 ? 1.0 : col[(size_t)r * n];
+      Yb[(size_t)r * m + j] -= vr * w[j];
+    }
+    __syncthreads();
+  }
 }
 
 }  // namespace dxtb

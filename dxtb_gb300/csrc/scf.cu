@@ -17,7 +17,9 @@
 namespace dxtb {
 
 constexpr int kScfThreads = 256;
-constexpr int kHist = 6;  // Anderson history length
+constexpr int kHist = 8;          // Anderson history length
+constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
+constexpr double kOccCut = 1e-15; // orbitals below this occupation carry no density
 
 struct MolView {
   int m, n, nat, nsh, N;
@@ -27,12 +29,13 @@ struct MolView {
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat;
+  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8;
 }
 
 struct Ws {
   double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
-  double *vsh_tmp;
+  double *vsh_tmp, *lu;
+  int *cl;
 };
 
 __device__ inline Ws ws_carve(double *base, int n, int nat) {
@@ -56,13 +59,16 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.g = q; q += N;
   w.hx = q; q += (size_t)kHist * N;
   w.hr = q; q += (size_t)kHist * N;
+  w.lu = q; q += (size_t)5 * n * kScfThreads;
+  w.cl = reinterpret_cast<int *>(q); q += n + 8;
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
 
 // Fermi-Dirac occupations of singly occupied orbitals summing to nel
-// (filling.py:428-742 converges to the same unique root). Bisection on the
-// electron count, warp 0 only. Returns false on failure.
+// (filling.py:428-742 converges to the same unique root): Newton steps on
+// the electron count, safeguarded by a bisection bracket; warp 0 only.
+// eps is sorted ascending. Returns false on failure.
 __device__ bool fermi_warp(int n, const double *eps, double nel, double kt, double *f) {
   const int lane = threadIdx.x & 31;
   if (nel <= 0.0) {
@@ -73,26 +79,27 @@ __device__ bool fermi_warp(int n, const double *eps, double nel, double kt, doub
     for (int j = lane; j < n; j += 32) f[j] = 1.0;
     return true;
   }
-  double emin = 1e308, emax = -1e308;
-  for (int j = lane; j < n; j += 32) {
-    emin = fmin(emin, eps[j]);
-    emax = fmax(emax, eps[j]);
-  }
-  emin = -warp_max(-emin);
-  emax = warp_max(emax);
-  double lo = emin - 60.0 * kt, hi = emax + 60.0 * kt;
+  double lo = eps[0] - 60.0 * kt, hi = eps[n - 1] + 60.0 * kt;
+  const int khomo = min(max((int)ceil(nel) - 1, 0), n - 1);
+  double mu = 0.5 * (eps[khomo] + eps[min(khomo + 1, n - 1)]);
+  const double ikt = 1.0 / kt;
   for (int it = 0; it < 200; ++it) {
-    const double mu = 0.5 * (lo + hi);
-    double s = 0.0;
+    double s = 0.0, ds = 0.0;
     for (int j = lane; j < n; j += 32) {
-      const double x = (eps[j] - mu) / kt;
-      s += x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+      const double x = (eps[j] - mu) * ikt;
+      const double v = x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+      s += v;
+      ds += v * (1.0 - v);
     }
-    s = warp_sum(s);
-    if (s > nel) hi = mu; else lo = mu;
-    if (hi - lo < 1e-16 * fmax(1.0, fabs(mu))) break;
+    s = warp_sum(s) - nel;
+    ds = warp_sum(ds) * ikt;
+    if (fabs(s) < 1e-13 * fmax(1.0, nel)) break;
+    if (s > 0.0) hi = mu; else lo = mu;
+    double next = ds > 0.0 ? mu - s / ds : 0.5 * (lo + hi);
+    if (!(next > lo && next < hi)) next = 0.5 * (lo + hi);
+    if (hi - lo < 1e-15 * fmax(1.0, fabs(mu))) break;
+    mu = next;
   }
-  const double mu = 0.5 * (lo + hi);
   double s = 0.0;
   for (int j = lane; j < n; j += 32) {
     const double x = (eps[j] - mu) / kt;
@@ -238,7 +245,8 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
 
 __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
   __shared__ double red[32];
-  __shared__ int s_flag;
+  __shared__ int s_flag, s_m, s_ncl;
+  __shared__ double s_tri[2 * kSmemTri];
   const dxtb_batch &b = a.b;
   MolView mv;
   mv.m = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
@@ -274,7 +282,7 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
   // ---- orthogonaliser X = L^-1 (S = L L^T), once per geometry ----
   for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = S[t];
   __syncthreads();
-  if (!cta_cholesky(n, w.A, red)) status = DXTB_ERR_NOT_POSDEF;
+  if (!cta_cholesky(n, w.A)) status = DXTB_ERR_NOT_POSDEF;
   if (status == DXTB_OK) cta_trinv(n, w.A, w.Linv);
 
   for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = 0.0;
@@ -305,37 +313,72 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
     }
     __syncthreads();
     // ---- F' = X F X^T (exlibs/xitorch/_impls/linalg/symeig.py:57-61) ----
-    cta_gemm<false, false>(n, n, n, 1.0, w.Linv, n, w.Zt, n, 0.0, w.A, n);   // A = X F
-    cta_gemm<false, true>(n, n, n, 1.0, w.A, n, w.Linv, n, 0.0, w.Zt, n);    // Zt = (X F) X^T
-    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = w.Zt[t];
-    __syncthreads();
-    // ---- eigensolve: Householder tridiagonalisation + implicit QL ----
-    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, red);
-    cta_form_q(n, w.A, w.tau, C, w.Zt, w.p);  // C used as scratch
-    if (!cta_tql(n, w.d, w.e, w.Zt, w.rc, w.rs)) {
-      status = DXTB_ERR_NAN;
-      break;
+    // X = L^-1 is lower triangular: A = X F needs k <= i; only the lower
+    // triangle of (X F) X^T is formed (k <= j), then mirrored.
+    cta_gemm<false, false>(n, n, n, 1.0, w.Linv, n, w.Zt, n, 0.0, w.A, n, kALower);
+    cta_gemm<false, true>(n, n, n, 1.0, w.A, n, w.Linv, n, 0.0, w.Zt, n, kBLowerT, true);
+    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+      const int i = (int)(t / n), j = (int)(t % n);
+      w.A[t] = j <= i ? w.Zt[t] : w.Zt[(size_t)j * n + i];
     }
-    for (int j = threadIdx.x; j < n; j += blockDim.x) w.eps[j] = w.d[j];
-    // ---- C^T = Zt X (orbital j is row j) ----
-    cta_gemm<false, false>(n, n, n, 1.0, w.Zt, n, w.Linv, n, 0.0, C, n);
+    __syncthreads();
+    // ---- eigenvalues: Householder tridiagonalisation + implicit QL ----
+    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, red);
+    {
+      double *sd = n <= kSmemTri ? s_tri : w.rs;
+      double *se = n <= kSmemTri ? s_tri + kSmemTri : w.vsh_tmp;
+      if (!cta_tql_values(n, w.d, w.e, sd, se, w.rc)) {
+        status = DXTB_ERR_NAN;
+        break;
+      }
+    }
+    cta_rank_sort(n, w.rc, w.eps);  // ascending, like eigh
     // ---- Fermi occupations (filling.py:428-742), both spin channels ----
     if (threadIdx.x < 32) {
       bool ok = fermi_warp(n, w.eps, nel_a, a.kt, w.fa);
-      ok = ok && fermi_warp(n, w.eps, nel_b, a.kt, w.fb);
-      if (threadIdx.x == 0) s_flag = ok ? 1 : 0;
+      if (nel_b == nel_a) {
+        for (int j = threadIdx.x; j < n; j += 32) w.fb[j] = w.fa[j];
+      } else {
+        ok = ok && fermi_warp(n, w.eps, nel_b, a.kt, w.fb);
+      }
+      __syncwarp();
+      if (threadIdx.x == 0) {
+        s_flag = ok ? 1 : 0;
+        // orbitals with non-vanishing occupation (occupations decrease with j)
+        int mv_ = 0;
+        while (mv_ < n && w.fa[mv_] + w.fb[mv_] > kOccCut) ++mv_;
+        s_m = mv_ > 0 ? mv_ : 1;
+      }
     }
     __syncthreads();
     if (!s_flag) {
       status = DXTB_ERR_FERMI;
       break;
     }
+    // ---- eigenvectors of the m lowest orbitals only ----
+    double tnorm = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) tnorm = fmax(tnorm, fabs(w.d[j]) + 2.0 * fabs(w.e[j]));
+    tnorm = block_max(tnorm, red);
+    if (threadIdx.x == 0) {
+      // keep a whole eigenvalue cluster together
+      int mm = s_m;
+      const double ctol = 1e-6 * fmax(tnorm, 1.0);
+      while (mm < n && w.eps[mm] - w.eps[mm - 1] <= ctol) ++mm;
+      s_m = mm;
+    }
+    __syncthreads();
+    const int mo = s_m;
+    cta_tri_vectors(n, w.d, w.e, w.eps, mo, tnorm, w.Zt, w.lu, w.cl, &s_ncl);
+    cta_back_transform(n, w.A, w.tau, w.Zt, mo, w.p);
+    // ---- C^T = Y^T X (orbital j is row j; X lower -> k >= i) ----
+    cta_gemm<true, false>(mo, n, n, 1.0, w.Zt, mo, w.Linv, n, 0.0, C, n, kBUpper);
     for (int j = threadIdx.x; j < n; j += blockDim.x) w.p[j] = w.fa[j] + w.fb[j];
     __syncthreads();
     // ---- density P = C diag(occ) C^T (scf/utils.py:29-52) ----
-    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = C[t] * w.p[t / n];
+    for (int64_t t = threadIdx.x; t < (int64_t)mo * n; t += blockDim.x) w.A[t] = C[t] * w.p[t / n];
     __syncthreads();
-    cta_gemm<true, false>(n, n, n, 1.0, C, n, w.A, n, 0.0, P, n);
+    cta_gemm<true, false>(n, n, mo, 1.0, C, n, w.A, n, 0.0, P, n, kFull, true);
+    cta_mirror_lower(n, P);
     // ---- Mulliken charges and atomic multipoles (conversions.py:203-251) ----
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       double pop = 0.0;
@@ -495,13 +538,17 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
         a.qp[6 * mv.a0 + t] = qpa[t];
       }
     }
-    // energy-weighted density W = C diag(occ eps) C^T
+    // energy-weighted density W = C diag(occ eps) C^T over the m orbitals
+    const int mo = s_m;
     if (a.W != nullptr) {
-      for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x)
+      for (int64_t t = threadIdx.x; t < (int64_t)mo * n; t += blockDim.x)
         w.A[t] = C[t] * (w.fa[t / n] + w.fb[t / n]) * w.eps[t / n];
       __syncthreads();
-      cta_gemm<true, false>(n, n, n, 1.0, C, n, w.A, n, 0.0, a.W + mv.moff, n);
+      cta_gemm<true, false>(n, n, mo, 1.0, C, n, w.A, n, 0.0, a.W + mv.moff, n, kFull, true);
+      cta_mirror_lower(n, a.W + mv.moff);
     }
+    // coefficients of orbitals without occupation are not computed
+    for (int64_t t = (int64_t)mo * n + threadIdx.x; t < (int64_t)n * n; t += blockDim.x) C[t] = 0.0;
   }
   if (threadIdx.x == 0) a.status[m] = status;
 }
