@@ -159,12 +159,26 @@ __device__ void cta_tridiag(int n, double *A, double *d, double *e, double *tau,
       d[k] = A[(size_t)k * n + k];
     }
     if (t != 0.0) {
-      // p = t * A22 v (v[0] = 1, v[r] = col[r*n])
+      // p = t * A22 v (v[0] = 1, v[r] = col[r*n]); A22 is symmetric, so row
+      // r of the product reads column r (coalesced over r). The c range is
+      // split into G groups so that all threads work; partials in smem.
       const double *A22 = A + (size_t)(k + 1) * n + (k + 1);
-      for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        double s = A22[r];  // c = 0, v0 = 1 (A22 symmetric: A22[c][r])
-        for (int c = 1; c < m; ++c) s = fma(A22[(size_t)c * n + r], col[(size_t)c * n], s);
-        p[r] = t * s;
+      __shared__ double s_part[256];
+      const int G = m < (int)blockDim.x ? min(256 / m, (int)blockDim.x / m) : 1;
+      for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
+        const int r = q % m, g = q / m;
+        double s = 0.0;
+        for (int c = g; c < m; c += G)
+          s = fma(A22[(size_t)c * n + r], c == 0 ? 1.0 : col[(size_t)c * n], s);
+        if (G > 1) s_part[g * m + r] = s; else p[r] = t * s;
+      }
+      __syncthreads();
+      if (G > 1) {
+        for (int r = threadIdx.x; r < m; r += blockDim.x) {
+          double s = 0.0;
+          for (int g = 0; g < G; ++g) s += s_part[g * m + r];
+          p[r] = t * s;
+        }
       }
       __syncthreads();
       double part2 = 0.0;
@@ -265,6 +279,145 @@ __device__ bool cta_tql_values(int n, const double *d, const double *e, double *
   return s_ok != 0;
 }
 
+// Number of eigenvalues of the tridiagonal (d, e) below x (Sturm count of
+// the LDL^T pivots, zero pivots replaced by -tiny), in float32.
+__device__ __forceinline__ int sturm_count_f32(int n, const float *d, const float *e2, float x,
+                                               float tiny) {
+  int cnt = 0;
+  float q = d[0] - x;
+  if (q == 0.0f) q = -tiny;
+  cnt += q < 0.0f;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - e2[i - 1] / q;
+    if (q == 0.0f) q = -tiny;
+    cnt += q < 0.0f;
+  }
+  return cnt;
+}
+
+// The same count in float64 (robust fallback).
+__device__ __forceinline__ int sturm_count_f64(int n, const double *d, const double *e, double x,
+                                               double tiny) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (q == 0.0) q = -tiny;
+  cnt += q < 0.0;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
+    if (q == 0.0) q = -tiny;
+    cnt += q < 0.0;
+  }
+  return cnt;
+}
+
+// Characteristic polynomial p(x) = det(T - x I) of the leading principal
+// minors and its derivative, by the three-term recurrence with rescaling
+// (no divisions); returns p / p' (the Newton correction is -p/p').
+__device__ __forceinline__ double charpoly_ratio(int n, const double *d, const double *e, double x) {
+  double p0 = 1.0, p1 = d[0] - x;   // p_{k-1}, p_k
+  double q0 = 0.0, q1 = -1.0;       // p'_{k-1}, p'_k
+  for (int i = 1; i < n; ++i) {
+    const double di = d[i] - x, e2 = e[i - 1] * e[i - 1];
+    const double p2 = di * p1 - e2 * p0;
+    const double q2 = -p1 + di * q1 - e2 * q0;
+    p0 = p1;
+    p1 = p2;
+    q0 = q1;
+    q1 = q2;
+    const double big = fmax(fabs(p1), fabs(q1));
+    if (big > 1e150) {
+      p0 *= 1e-150; p1 *= 1e-150; q0 *= 1e-150; q1 *= 1e-150;
+    } else if (big < 1e-150 && big > 0.0) {
+      p0 *= 1e150; p1 *= 1e150; q0 *= 1e150; q1 *= 1e150;
+    }
+  }
+  return q1 != 0.0 ? p1 / q1 : 0.0;
+}
+
+// All eigenvalues of the symmetric tridiagonal (d, e), ascending, one per
+// thread: float32 bisection on Sturm counts isolates eigenvalue k to ~1e-7
+// relative, float64 Newton steps on the characteristic polynomial refine it,
+// and a float64 Sturm count checks that the result is the k-th eigenvalue;
+// eigenvalues that fail (clusters closer than the float32 resolution) are
+// recomputed by float64 bisection. df/e2f: float scratch of n each.
+__device__ void cta_tri_eigenvalues(int n, const double *d, const double *e, double *lam,
+                                    float *df, float *e2f) {
+  __shared__ double s_gl, s_gu;
+  double gl = 1e308, gu = -1e308;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
+    gl = fmin(gl, d[i] - r);
+    gu = fmax(gu, d[i] + r);
+    df[i] = (float)d[i];
+    e2f[i] = i < n - 1 ? (float)(e[i] * e[i]) : 0.0f;
+  }
+  gl = -warp_max(-gl);
+  gu = warp_max(gu);
+  if (threadIdx.x == 0) {
+    s_gl = gl;
+    s_gu = gu;
+  }
+  __syncthreads();
+  for (int w = 1; w < (int)((blockDim.x + 31) >> 5); ++w) {
+    // fold the other warps' bounds (small loop, no extra shared array)
+    __syncthreads();
+    if ((threadIdx.x >> 5) == w && (threadIdx.x & 31) == 0) {
+      s_gl = fmin(s_gl, gl);
+      s_gu = fmax(s_gu, gu);
+    }
+  }
+  __syncthreads();
+  const double tnorm = fmax(fabs(s_gl), fabs(s_gu));
+  const double span = s_gu - s_gl;
+  const double glo = s_gl - 1e-6 * span - 1e-12, ghi = s_gu + 1e-6 * span + 1e-12;
+  const float tinyf = 1e-30f;
+  const double tiny = 1e-300;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    // --- float32 bisection: count(lo) <= k < count(hi) ---
+    float lo = (float)glo, hi = (float)ghi;
+    for (int it = 0; it < 60; ++it) {
+      const float mid = 0.5f * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      if (sturm_count_f32(n, df, e2f, mid, tinyf) <= k) lo = mid; else hi = mid;
+    }
+    const double w32 = fmax((double)hi - (double)lo, 4e-7 * tnorm + 1e-12);
+    double x = 0.5 * ((double)lo + (double)hi);
+    const double blo = x - 4.0 * w32, bhi = x + 4.0 * w32;
+    // --- float64 Newton on p(x) ---
+    bool ok = true;
+    for (int it = 0; it < 4; ++it) {
+      const double dx = charpoly_ratio(n, d, e, x);
+      x -= dx;
+      if (!(x > blo && x < bhi)) { ok = false; break; }
+      if (fabs(dx) <= 2.0 * kEps * fmax(fabs(x), 1e-3 * tnorm)) break;
+    }
+    // --- check the index with float64 Sturm counts (eigenvalues closer than
+    // del are interchangeable: their vectors come from one cluster) ---
+    const double del = 1e-12 * fmax(tnorm, 1.0);
+    if (ok) {
+      const int cl = sturm_count_f64(n, d, e, x - del, tiny);
+      const int ch = sturm_count_f64(n, d, e, x + del, tiny);
+      ok = (cl <= k && k < ch);
+    }
+    if (!ok) {
+      // --- float64 bisection inside the float32 bracket (widened) ---
+      double l = glo, h = ghi;
+      if (sturm_count_f64(n, d, e, blo, tiny) <= k && sturm_count_f64(n, d, e, bhi, tiny) > k) {
+        l = blo;
+        h = bhi;
+      }
+      for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (l + h);
+        if (mid <= l || mid >= h) break;
+        if (sturm_count_f64(n, d, e, mid, tiny) <= k) l = mid; else h = mid;
+      }
+      x = 0.5 * (l + h);
+    }
+    lam[k] = x;
+  }
+  __syncthreads();
+}
+
 // Ascending sort by rank (ties broken by index): out[rank(i)] = in[i].
 __device__ void cta_rank_sort(int n, const double *in, double *out) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -345,11 +498,15 @@ __device__ void cta_tri_vectors(int n, const double *d, const double *e, const d
           bsup = -mult * en;
         }
       }
-      LU(U0, n - 1) = fabs(a) < tiny ? copysign(tiny, a == 0.0 ? 1.0 : a) : a;
-      for (int i = 0; i < n - 1; ++i)
-        if (fabs(LU(U0, i)) < tiny) LU(U0, i) = copysign(tiny, LU(U0, i) == 0.0 ? 1.0 : LU(U0, i));
+      LU(U0, n - 1) = a;
+      // tiny pivots perturbed (sign kept); U0 then holds the reciprocals
+      for (int i = 0; i < n; ++i) {
+        const double u = LU(U0, i);
+        LU(U0, i) = 1.0 / (fabs(u) < tiny ? copysign(tiny, u == 0.0 ? 1.0 : u) : u);
+      }
       for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
-      for (int it = 0; it < 3; ++it) {
+      const int nsolve = (j1 - j0 > 1) ? 3 : 2;
+      for (int it = 0; it < nsolve; ++it) {
         // forward: apply the row interchanges and multipliers
         for (int i = 0; i < n - 1; ++i) {
           double xi = Y[(size_t)i * m + j], xn = Y[(size_t)(i + 1) * m + j];
@@ -364,7 +521,7 @@ __device__ void cta_tri_vectors(int n, const double *d, const double *e, const d
         // back substitution with the upper factor (two super-diagonals)
         double x1 = 0.0, x2 = 0.0;
         for (int i = n - 1; i >= 0; --i) {
-          const double v = (Y[(size_t)i * m + j] - LU(U1, i) * x1 - LU(U2, i) * x2) / LU(U0, i);
+          const double v = (Y[(size_t)i * m + j] - LU(U1, i) * x1 - LU(U2, i) * x2) * LU(U0, i);
           Y[(size_t)i * m + j] = v;
           x2 = x1;
           x1 = v;
@@ -396,12 +553,24 @@ __device__ void cta_back_transform(int n, const double *A, const double *tau, do
     const int mm = n - k - 1;
     const double *col = A + (size_t)(k + 1) * n + k;
     double *Yb = Y + (size_t)(k + 1) * m;
-    for (int j = threadIdx.x; j < m; j += blockDim.x) {
-      double s = Yb[j];
-      for (int r = 1; r < mm; ++r) s = fma(col[(size_t)r * n], Yb[(size_t)r * m + j], s);
-      w[j] = t * s;
+    // w_j = t * v . Y[:, j]; the r range split into G groups (all threads busy)
+    __shared__ double s_bpart[256];
+    const int G = m < (int)blockDim.x ? min(256 / m, (int)blockDim.x / m) : 1;
+    for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
+      const int j = q % m, g = q / m;
+      double s = 0.0;
+      for (int r = g; r < mm; r += G) s = fma(r == 0 ? 1.0 : col[(size_t)r * n], Yb[(size_t)r * m + j], s);
+      if (G > 1) s_bpart[g * m + j] = s; else w[j] = t * s;
     }
     __syncthreads();
+    if (G > 1) {
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        double s = 0.0;
+        for (int g = 0; g < G; ++g) s += s_bpart[g * m + j];
+        w[j] = t * s;
+      }
+      __syncthreads();
+    }
     for (int64_t q = threadIdx.x; q < (int64_t)mm * m; q += blockDim.x) {
       const int r = (int)(q / m), j = (int)(q % m);
       const double vr = r == 0 ? 1.0 : col[(size_t)r * n];

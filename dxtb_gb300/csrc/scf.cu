@@ -17,7 +17,7 @@
 namespace dxtb {
 
 constexpr int kScfThreads = 256;
-constexpr int kHist = 8;          // Anderson history length
+constexpr int kHist = 16;         // Anderson history length
 constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
 constexpr double kOccCut = 1e-15; // orbitals below this occupation carry no density
 
@@ -29,12 +29,13 @@ struct MolView {
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8;
+  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8 +
+         2 * kHist * kHist + 8 * kHist + 64;
 }
 
 struct Ws {
   double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
-  double *vsh_tmp, *lu;
+  double *vsh_tmp, *lu, *anderson;
   int *cl;
 };
 
@@ -61,6 +62,7 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.hr = q; q += (size_t)kHist * N;
   w.lu = q; q += (size_t)5 * n * kScfThreads;
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
+  w.anderson = q; q += 2 * kHist * kHist + 8 * kHist + 64;
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
@@ -243,7 +245,7 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
   return block_sum(e, red);
 }
 
-__global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
+__global__ void __launch_bounds__(kScfThreads, 2) k_scf(ScfArgs a) {
   __shared__ double red[32];
   __shared__ int s_flag, s_m, s_ncl;
   __shared__ double s_tri[2 * kSmemTri];
@@ -270,7 +272,6 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
   Ws w = ws_carve(a.ws + a.ws_off[m], n, nat);
   double *qsh = w.misc, *qat = qsh + mv.nsh + 1, *vat = qat + nat + 1;
   double *dpa = vat + nat + 1, *qpa = dpa + 3 * nat + 1, *qo = qpa + 6 * nat + 1;
-  double *amat = qo + n + 1;  // Anderson normal equations (kHist^2 + kHist)
   double *vsh = w.vsh_tmp;
 
   const double *S = a.S + mv.moff, *H0 = a.H0 + mv.moff;
@@ -325,12 +326,10 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
     // ---- eigenvalues: Householder tridiagonalisation + implicit QL ----
     cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, red);
     {
-      double *sd = n <= kSmemTri ? s_tri : w.rs;
-      double *se = n <= kSmemTri ? s_tri + kSmemTri : w.vsh_tmp;
-      if (!cta_tql_values(n, w.d, w.e, sd, se, w.rc)) {
-        status = DXTB_ERR_NAN;
-        break;
-      }
+      float *df = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) : reinterpret_cast<float *>(w.rs);
+      float *e2f = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) + 2 * kSmemTri
+                                     : reinterpret_cast<float *>(w.vsh_tmp);
+      cta_tri_eigenvalues(n, w.d, w.e, w.rc, df, e2f);
     }
     cta_rank_sort(n, w.rc, w.eps);  // ascending, like eigh
     // ---- Fermi occupations (filling.py:428-742), both spin channels ----
@@ -416,87 +415,99 @@ __global__ void __launch_bounds__(kScfThreads) k_scf(ScfArgs a) {
       break;
     }
     // ---- Anderson mixing of the potential (scf/mixer/anderson.py) ----
-    // history: hx[k] = x_k, hr[k] = r_k = G(x_k) - x_k (ring buffer)
-    double *hxk = w.hx + (size_t)hpos * N, *hrk = w.hr + (size_t)hpos * N;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
-      hxk[t] = w.x[t];
-      hrk[t] = w.g[t] - w.x[t];
+    // Ring buffer of (x_k, r_k = G(x_k) - x_k) with the Gram matrix
+    // R[s][t] = r_s . r_t kept up to date: one fused pass per iteration
+    // computes the new residual's products with every stored one.
+    {
+      double *hxk = w.hx + (size_t)hpos * N, *hrk = w.hr + (size_t)hpos * N;
+      const int nvalid = min(nhist + 1, kHist);
+      double acc[kHist];
+#pragma unroll
+      for (int s = 0; s < kHist; ++s) acc[s] = 0.0;
+      for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        const double rn = w.g[t] - w.x[t];
+        hxk[t] = w.x[t];
+        hrk[t] = rn;
+#pragma unroll
+        for (int s = 0; s < kHist; ++s)
+          if (s < nvalid) acc[s] += rn * w.hr[(size_t)s * N + t];
+      }
+      // block reduction of the kHist partial sums
+      double *gram = w.anderson;                 // [kHist][kHist]
+      double *wred = gram + kHist * kHist;       // [8 warps][kHist]
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+      for (int s = 0; s < kHist; ++s) {
+        const double v = warp_sum(acc[s]);
+        if (lane == 0) wred[wid * kHist + s] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x < nvalid) {
+        double v = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += wred[q * kHist + threadIdx.x];
+        gram[hpos * kHist + threadIdx.x] = v;
+        gram[threadIdx.x * kHist + hpos] = v;
+      }
+      __syncthreads();
     }
-    __syncthreads();
     nhist = min(nhist + 1, kHist);
     const int newest = hpos;
     hpos = (hpos + 1) % kHist;
     const int mm = nhist - 1;  // number of differences
+    double *hrk = w.hr + (size_t)newest * N;
     if (mm == 0) {
       for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] += beta_mix * hrk[t];
     } else {
-      // differences relative to the newest: dR_k = r_newest - r_k, dX_k = x_newest - x_k
-      // normal equations (dR^T dR) gam = dR^T r_newest
+      // differences to the newest: dR_u = r_n - r_u, dX_u = x_n - x_u;
+      // normal equations (dR^T dR) gam = dR^T r_n from the Gram matrix
       int idx[kHist];
-      int c = 0;
-      for (int k = 0; k < kHist && c < mm; ++k) {
-        const int slot = (newest - 1 - k + 2 * kHist) % kHist;
-        idx[c++] = slot;
-      }
-      for (int u = 0; u < mm; ++u) {
-        const double *ru = w.hr + (size_t)idx[u] * N;
-        for (int v = u; v <= mm; ++v) {
-          const double *rv = v < mm ? w.hr + (size_t)idx[v] * N : nullptr;
-          double s = 0.0;
-          for (int t = threadIdx.x; t < N; t += blockDim.x) {
-            const double du = hrk[t] - ru[t];
-            const double dv = v < mm ? hrk[t] - rv[t] : hrk[t];
-            s += du * dv;
-          }
-          s = block_sum(s, red);
-          if (threadIdx.x == 0) {
-            if (v < mm) {
-              amat[u * kHist + v] = s;
-              amat[v * kHist + u] = s;
-            } else {
-              amat[kHist * kHist + u] = s;
-            }
-          }
-        }
-      }
-      __syncthreads();
+      for (int u = 0; u < mm; ++u) idx[u] = (newest - 1 - u + 2 * kHist) % kHist;
+      const double *gram = w.anderson;
+      double *gam = w.anderson + kHist * kHist + 8 * kHist;
       if (threadIdx.x == 0) {
-        // Gaussian elimination with partial pivoting, Tikhonov shift
         double M[kHist][kHist + 1];
+        const double rnn = gram[newest * kHist + newest];
         double tr = 0.0;
-        for (int u = 0; u < mm; ++u) tr += amat[u * kHist + u];
         for (int u = 0; u < mm; ++u) {
-          for (int v = 0; v < mm; ++v) M[u][v] = amat[u * kHist + v];
-          M[u][u] += 1e-12 * tr + 1e-300;
-          M[u][mm] = amat[kHist * kHist + u];
+          const double rnu = gram[newest * kHist + idx[u]];
+          for (int v = 0; v < mm; ++v) {
+            const double rnv = gram[newest * kHist + idx[v]];
+            M[u][v] = rnn - rnu - rnv + gram[idx[u] * kHist + idx[v]];
+          }
+          M[u][mm] = rnn - rnu;
+          tr += M[u][u];
         }
+        for (int u = 0; u < mm; ++u) M[u][u] += 1e-12 * tr + 1e-300;
+        // Gaussian elimination with partial pivoting
         for (int col = 0; col < mm; ++col) {
           int piv = col;
           for (int r = col + 1; r < mm; ++r)
             if (fabs(M[r][col]) > fabs(M[piv][col])) piv = r;
-          for (int v = 0; v <= mm; ++v) {
-            const double tmp = M[col][v];
-            M[col][v] = M[piv][v];
-            M[piv][v] = tmp;
-          }
+          if (piv != col)
+            for (int v = 0; v <= mm; ++v) {
+              const double tmp = M[col][v];
+              M[col][v] = M[piv][v];
+              M[piv][v] = tmp;
+            }
+          const double ip = 1.0 / M[col][col];
           for (int r = col + 1; r < mm; ++r) {
-            const double f = M[r][col] / M[col][col];
+            const double f = M[r][col] * ip;
             for (int v = col; v <= mm; ++v) M[r][v] -= f * M[col][v];
           }
         }
         for (int r = mm - 1; r >= 0; --r) {
           double s = M[r][mm];
-          for (int v = r + 1; v < mm; ++v) s -= M[r][v] * amat[kHist * kHist + kHist + v];
-          amat[kHist * kHist + kHist + r] = s / M[r][r];
+          for (int v = r + 1; v < mm; ++v) s -= M[r][v] * gam[v];
+          gam[r] = s / M[r][r];
         }
       }
       __syncthreads();
-      const double *gam = amat + kHist * kHist + kHist;
       for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        double xn = w.x[t] + beta_mix * hrk[t];
+        const double xt = w.x[t], rt = hrk[t];
+        double xn = xt + beta_mix * rt;
         for (int u = 0; u < mm; ++u) {
-          const double *xu = w.hx + (size_t)idx[u] * N, *ru = w.hr + (size_t)idx[u] * N;
-          xn -= gam[u] * ((w.x[t] - xu[t]) + beta_mix * (hrk[t] - ru[t]));
+          const size_t o = (size_t)idx[u] * N + t;
+          xn -= gam[u] * ((xt - w.hx[o]) + beta_mix * (rt - w.hr[o]));
         }
         w.x[t] = xn;
       }
