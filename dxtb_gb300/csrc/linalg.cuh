@@ -17,6 +17,8 @@
 namespace dxtb {
 
 // Shapes of the k-loop for triangular operands.
+constexpr int kTriSmem = 512;  // Householder vectors in shared memory up to this order
+
 enum KRange : int {
   kFull = 0,     // k in [0, K)
   kALower = 1,   // op(A)(i,k) = 0 for k > i   -> k < i0 + 4
@@ -133,66 +135,78 @@ __device__ void cta_trinv(int n, const double *L, double *X) {
 // sub-diagonal (e[i] couples i and i+1), the reflector of step k is stored
 // in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k].
 __device__ void cta_tridiag(int n, double *A, double *d, double *e, double *tau, double *p,
-                            double *red) {
+                            double *vbuf, double *red) {
+  // The Householder vector and p live in shared memory when they fit.
+  __shared__ double s_v[kTriSmem], s_p[kTriSmem];
+  __shared__ double s_part[256];
+  double *sv = n <= kTriSmem ? s_v : vbuf;
+  double *sp = n <= kTriSmem ? s_p : p;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
     double *col = A + (size_t)(k + 1) * n + k;  // col[r*n], r < m
     double part = 0.0;
-    for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) {
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
       const double x = col[(size_t)r * n];
-      part += x * x;
+      sv[r] = x;
+      if (r > 0) part += x * x;
     }
-    const double sigma = block_sum(part, red);
-    const double alpha = col[0];
+    const double sigma = block_sum(part, red);  // also orders the sv writes
+    const double alpha = col[0];  // not sv[0]: thread 0 overwrites it below
     double t = 0.0, beta = alpha;
     if (sigma > 0.0) {
       const double nrm = sqrt(alpha * alpha + sigma);
       beta = alpha >= 0.0 ? -nrm : nrm;
       t = (beta - alpha) / beta;
       const double scale = 1.0 / (alpha - beta);
-      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) col[(size_t)r * n] *= scale;
+      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) {
+        const double v = sv[r] * scale;
+        sv[r] = v;
+        col[(size_t)r * n] = v;  // kept for the back-transformation
+      }
     }
-    __syncthreads();
     if (threadIdx.x == 0) {
+      sv[0] = 1.0;
       tau[k] = t;
       e[k] = beta;
       d[k] = A[(size_t)k * n + k];
     }
+    __syncthreads();
     if (t != 0.0) {
-      // p = t * A22 v (v[0] = 1, v[r] = col[r*n]); A22 is symmetric, so row
-      // r of the product reads column r (coalesced over r). The c range is
-      // split into G groups so that all threads work; partials in smem.
+      // p = t * A22 v; A22 is symmetric, so row r of the product reads
+      // column r (coalesced over r). The c range is split into G groups so
+      // that all threads work; partials in smem, p^T v fused in.
       const double *A22 = A + (size_t)(k + 1) * n + (k + 1);
-      __shared__ double s_part[256];
       const int G = m < (int)blockDim.x ? min(256 / m, (int)blockDim.x / m) : 1;
       for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
         const int r = q % m, g = q / m;
         double s = 0.0;
-        for (int c = g; c < m; c += G)
-          s = fma(A22[(size_t)c * n + r], c == 0 ? 1.0 : col[(size_t)c * n], s);
-        if (G > 1) s_part[g * m + r] = s; else p[r] = t * s;
-      }
-      __syncthreads();
-      if (G > 1) {
-        for (int r = threadIdx.x; r < m; r += blockDim.x) {
-          double s = 0.0;
-          for (int g = 0; g < G; ++g) s += s_part[g * m + r];
-          p[r] = t * s;
-        }
+        for (int c = g; c < m; c += G) s = fma(A22[(size_t)c * n + r], sv[c], s);
+        if (G > 1) s_part[g * m + r] = s; else sp[r] = t * s;
       }
       __syncthreads();
       double part2 = 0.0;
-      for (int r = threadIdx.x; r < m; r += blockDim.x)
-        part2 += p[r] * (r == 0 ? 1.0 : col[(size_t)r * n]);
+      for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        double pr;
+        if (G > 1) {
+          double s = 0.0;
+          for (int g = 0; g < G; ++g) s += s_part[g * m + r];
+          pr = t * s;
+          sp[r] = pr;
+        } else {
+          pr = sp[r];
+        }
+        part2 += pr * sv[r];
+      }
       const double K = 0.5 * t * block_sum(part2, red);
-      for (int r = threadIdx.x; r < m; r += blockDim.x) p[r] -= K * (r == 0 ? 1.0 : col[(size_t)r * n]);
+      for (int r = threadIdx.x; r < m; r += blockDim.x) sp[r] -= K * sv[r];
       __syncthreads();
+      // rank-2 update, rows over warps, columns over lanes (coalesced)
       double *W = A + (size_t)(k + 1) * n + (k + 1);
-      for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += blockDim.x) {
-        const int r = (int)(q / m), c = (int)(q % m);
-        const double vr = r == 0 ? 1.0 : col[(size_t)r * n];
-        const double vc = c == 0 ? 1.0 : col[(size_t)c * n];
-        W[(size_t)r * n + c] -= vr * p[c] + p[r] * vc;
+      for (int r = ty; r < m; r += nty) {
+        const double vr = sv[r], pr = sp[r];
+        double *Wr = W + (size_t)r * n;
+        for (int c = tx; c < m; c += 32) Wr[c] -= vr * sp[c] + pr * sv[c];
       }
     }
     __syncthreads();

@@ -17,7 +17,8 @@
 namespace dxtb {
 
 constexpr int kScfThreads = 256;
-constexpr int kHist = 16;         // Anderson history length
+constexpr int kRank = 64;         // rank of the Broyden inverse-Jacobian memory
+constexpr double kDamp = 0.5;     // step damping of the root solver (defaults.DAMP)
 constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
 constexpr double kOccCut = 1e-15; // orbitals below this occupation carry no density
 
@@ -29,13 +30,13 @@ struct MolView {
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kHist + 4) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8 +
-         2 * kHist * kHist + 8 * kHist + 64;
+  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8 +
+         4 * kRank + 64;
 }
 
 struct Ws {
   double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
-  double *vsh_tmp, *lu, *anderson;
+  double *vsh_tmp, *lu, *anderson, *xold, *rold, *xbest;
   int *cl;
 };
 
@@ -58,11 +59,14 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.vsh_tmp = q; q += n;
   w.x = q; q += N;
   w.g = q; q += N;
-  w.hx = q; q += (size_t)kHist * N;
-  w.hr = q; q += (size_t)kHist * N;
+  w.hx = q; q += (size_t)kRank * N;
+  w.hr = q; q += (size_t)kRank * N;
+  w.xold = q; q += N;
+  w.rold = q; q += N;
+  w.xbest = q; q += N;
   w.lu = q; q += (size_t)5 * n * kScfThreads;
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
-  w.anderson = q; q += 2 * kHist * kHist + 8 * kHist + 64;
+  w.anderson = q; q += 4 * kRank + 64;
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
@@ -123,7 +127,7 @@ struct ScfArgs {
   const double *pf;
   const int32_t *pi;
   const double *S, *H0, *D, *Q, *gamma, *hd, *sd, *dd, *sq, *gb, *n0, *nel;
-  double kt, tol;
+  double kt, xtol, ftol;
   int maxiter;
   const int64_t *ws_off;
   const int32_t *order;
@@ -289,9 +293,8 @@ __global__ void __launch_bounds__(kScfThreads, 2) k_scf(ScfArgs a) {
   for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = 0.0;
   __syncthreads();
 
-  int it = 0, nhist = 0, hpos = 0;
-  double resid = 0.0;
-  const double beta_mix = 0.4;
+  int it = 0, nrank = 0, final_eval = 0, hit_max = 0;
+  double resid = 0.0, best_ynorm = 1e308, dx_norm = 0.0;
   while (status == DXTB_OK) {
     ++it;
     // ---- Fock matrix F(x) into Zt (conversions.py:255-297) ----
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(kScfThreads, 2) k_scf(ScfArgs a) {
     }
     __syncthreads();
     // ---- eigenvalues: Householder tridiagonalisation + implicit QL ----
-    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, red);
+    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, w.rs, red);
     {
       float *df = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) : reinterpret_cast<float *>(w.rs);
       float *e2f = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) + 2 * kSmemTri
@@ -406,114 +409,121 @@ __global__ void __launch_bounds__(kScfThreads, 2) k_scf(ScfArgs a) {
     __syncthreads();
     // ---- new potential G(x) ----
     potential_from_charges(a, mv, qo, dpa, qpa, qsh, qat, vsh, vat, w.g, multipole, es3_shell);
-    double part = 0.0;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) part = fmax(part, fabs(w.g[t] - w.x[t]));
-    resid = block_max(part, red);
-    if (resid < a.tol) break;
-    if (it >= a.maxiter) {
-      status = DXTB_ERR_MAXITER;
+    if (final_eval) {
+      hit_max = 1;
       break;
     }
-    // ---- Anderson mixing of the potential (scf/mixer/anderson.py) ----
-    // Ring buffer of (x_k, r_k = G(x_k) - x_k) with the Gram matrix
-    // R[s][t] = r_s . r_t kept up to date: one fused pass per iteration
-    // computes the new residual's products with every stored one.
+    // ---- root solver on F(x) = x - G(x): limited-memory Broyden's first
+    // method on the inverse Jacobian, Gm = 0.5 I + sum_k c_k d_k^T, damped
+    // steps x += damp * dx, dx = -Gm F (the broyden1 of exlibs/xitorch/
+    // _impls/optimize/root/{rootsolver.py:42-265, _jacobian.py:51-120} with
+    // alpha = -0.5, damp = 0.5, line_search = False, scf/base.py:267-292);
+    // stop when |dx|_2 < x_tol and |F|_2 < f_tol. ----
     {
-      double *hxk = w.hx + (size_t)hpos * N, *hrk = w.hr + (size_t)hpos * N;
-      const int nvalid = min(nhist + 1, kHist);
-      double acc[kHist];
-#pragma unroll
-      for (int s = 0; s < kHist; ++s) acc[s] = 0.0;
-      for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        const double rn = w.g[t] - w.x[t];
-        hxk[t] = w.x[t];
-        hrk[t] = rn;
-#pragma unroll
-        for (int s = 0; s < kHist; ++s)
-          if (s < nvalid) acc[s] += rn * w.hr[(size_t)s * N + t];
-      }
-      // block reduction of the kHist partial sums
-      double *gram = w.anderson;                 // [kHist][kHist]
-      double *wred = gram + kHist * kHist;       // [8 warps][kHist]
+      double *sdot = w.anderson;                 // [kRank] dot products
+      double *sdot2 = sdot + kRank;              // [kRank]
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-      for (int s = 0; s < kHist; ++s) {
-        const double v = warp_sum(acc[s]);
-        if (lane == 0) wred[wid * kHist + s] = v;
-      }
-      __syncthreads();
-      if (threadIdx.x < nvalid) {
-        double v = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += wred[q * kHist + threadIdx.x];
-        gram[hpos * kHist + threadIdx.x] = v;
-        gram[threadIdx.x * kHist + hpos] = v;
-      }
-      __syncthreads();
-    }
-    nhist = min(nhist + 1, kHist);
-    const int newest = hpos;
-    hpos = (hpos + 1) % kHist;
-    const int mm = nhist - 1;  // number of differences
-    double *hrk = w.hr + (size_t)newest * N;
-    if (mm == 0) {
-      for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] += beta_mix * hrk[t];
-    } else {
-      // differences to the newest: dR_u = r_n - r_u, dX_u = x_n - x_u;
-      // normal equations (dR^T dR) gam = dR^T r_n from the Gram matrix
-      int idx[kHist];
-      for (int u = 0; u < mm; ++u) idx[u] = (newest - 1 - u + 2 * kHist) % kHist;
-      const double *gram = w.anderson;
-      double *gam = w.anderson + kHist * kHist + 8 * kHist;
-      if (threadIdx.x == 0) {
-        double M[kHist][kHist + 1];
-        const double rnn = gram[newest * kHist + newest];
-        double tr = 0.0;
-        for (int u = 0; u < mm; ++u) {
-          const double rnu = gram[newest * kHist + idx[u]];
-          for (int v = 0; v < mm; ++v) {
-            const double rnv = gram[newest * kHist + idx[v]];
-            M[u][v] = rnn - rnu - rnv + gram[idx[u] * kHist + idx[v]];
-          }
-          M[u][mm] = rnn - rnu;
-          tr += M[u][u];
-        }
-        for (int u = 0; u < mm; ++u) M[u][u] += 1e-12 * tr + 1e-300;
-        // Gaussian elimination with partial pivoting
-        for (int col = 0; col < mm; ++col) {
-          int piv = col;
-          for (int r = col + 1; r < mm; ++r)
-            if (fabs(M[r][col]) > fabs(M[piv][col])) piv = r;
-          if (piv != col)
-            for (int v = 0; v <= mm; ++v) {
-              const double tmp = M[col][v];
-              M[col][v] = M[piv][v];
-              M[piv][v] = tmp;
-            }
-          const double ip = 1.0 / M[col][col];
-          for (int r = col + 1; r < mm; ++r) {
-            const double f = M[r][col] * ip;
-            for (int v = col; v <= mm; ++v) M[r][v] -= f * M[col][v];
-          }
-        }
-        for (int r = mm - 1; r >= 0; --r) {
-          double s = M[r][mm];
-          for (int v = r + 1; v < mm; ++v) s -= M[r][v] * gam[v];
-          gam[r] = s / M[r][r];
-        }
-      }
-      __syncthreads();
+      const int nw = (int)(blockDim.x >> 5);
+      // |F|^2 with F = x - G(x)
+      double part = 0.0;
       for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        const double xt = w.x[t], rt = hrk[t];
-        double xn = xt + beta_mix * rt;
-        for (int u = 0; u < mm; ++u) {
-          const size_t o = (size_t)idx[u] * N + t;
-          xn -= gam[u] * ((xt - w.hx[o]) + beta_mix * (rt - w.hr[o]));
+        const double y = w.x[t] - w.g[t];
+        part += y * y;
+      }
+      const double ynorm = sqrt(block_sum(part, red));
+      resid = ynorm;
+      if (it == 1) {
+        if (ynorm <= a.ftol * kEps) break;
+        nrank = 0;
+      } else {
+        if (ynorm < best_ynorm) {
+          best_ynorm = ynorm;
+          for (int t = threadIdx.x; t < N; t += blockDim.x) w.xbest[t] = w.x[t];
         }
-        w.x[t] = xn;
+        // Broyden update with dx = x - x_prev, dy = F - F_prev:
+        // v = Gm^T dx, c = dx - Gm dy, d = v / (dy . v)
+        if (nrank >= kRank) nrank = 0;  // "restart" reduction of a full memory
+        for (int k = wid; k < 2 * nrank; k += nw) {
+          const int kk = k >> 1;
+          double s = 0.0;
+          if ((k & 1) == 0) {
+            const double *ck = w.hx + (size_t)kk * N;
+            for (int t = lane; t < N; t += 32) s += ck[t] * (w.x[t] - w.xold[t]);
+          } else {
+            const double *dk = w.hr + (size_t)kk * N;
+            for (int t = lane; t < N; t += 32) s += dk[t] * ((w.x[t] - w.g[t]) - w.rold[t]);
+          }
+          s = warp_sum(s);
+          if (lane == 0) {
+            if ((k & 1) == 0) sdot[kk] = s; else sdot2[kk] = s;
+          }
+        }
+        __syncthreads();
+        double *cn = w.hx + (size_t)nrank * N, *dn = w.hr + (size_t)nrank * N;
+        double pdv = 0.0;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+          const double dxt = w.x[t] - w.xold[t];
+          const double dyt = (w.x[t] - w.g[t]) - w.rold[t];
+          double v = 0.5 * dxt, gdy = 0.5 * dyt;
+          for (int k = 0; k < nrank; ++k) {
+            v += w.hr[(size_t)k * N + t] * sdot[k];
+            gdy += w.hx[(size_t)k * N + t] * sdot2[k];
+          }
+          cn[t] = dxt - gdy;
+          dn[t] = v;
+          pdv += dyt * v;
+        }
+        const double dyv = block_sum(pdv, red);
+        if (dyv == 0.0 || !isfinite(dyv)) {
+          status = DXTB_ERR_NAN;
+          break;
+        }
+        const double idyv = 1.0 / dyv;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) dn[t] *= idyv;
+        ++nrank;
+        __syncthreads();
+        if (dx_norm < a.xtol && ynorm < a.ftol) break;  // converged at x
+      }
+      if (it >= a.maxiter) {
+        // not converged: evaluate once more at the best iterate, which the
+        // root solver returns with a warning (rootsolver.py:250-259)
+        if (best_ynorm < ynorm) {
+          for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = w.xbest[t];
+          final_eval = 1;
+          __syncthreads();
+          continue;
+        }
+        hit_max = 1;
+        break;
+      }
+      // F_prev = F, x_prev = x; dx = -Gm F = -(0.5 F + sum_k c_k (d_k . F))
+      for (int k = wid; k < nrank; k += nw) {
+        const double *dk = w.hr + (size_t)k * N;
+        double s = 0.0;
+        for (int t = lane; t < N; t += 32) s += dk[t] * (w.x[t] - w.g[t]);
+        s = warp_sum(s);
+        if (lane == 0) sdot[k] = s;
+      }
+      __syncthreads();
+      double pdx = 0.0;
+      for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        const double y = w.x[t] - w.g[t];
+        double dx = -0.5 * y;
+        for (int k = 0; k < nrank; ++k) dx -= w.hx[(size_t)k * N + t] * sdot[k];
+        w.rold[t] = y;
+        w.xold[t] = w.x[t];
+        w.x[t] += kDamp * dx;
+        pdx += dx * dx;
+      }
+      dx_norm = sqrt(block_sum(pdx, red));
+      if (dx_norm == 0.0) {
+        status = DXTB_ERR_NAN;
+        break;
       }
     }
     __syncthreads();
   }
+  if (hit_max && status == DXTB_OK) status = DXTB_ERR_MAXITER;
 
   // ---- outputs ----
   if (status == DXTB_OK || status == DXTB_ERR_MAXITER) {
@@ -601,7 +611,8 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   a.n0 = n0;
   a.nel = nel;
   a.kt = kt;
-  a.tol = tol;
+  a.xtol = tol;  // x_atol and f_atol of the reference: one tolerance here
+  a.ftol = tol;
   a.maxiter = maxiter;
   a.ws_off = ws_off;
   a.order = order;

@@ -850,6 +850,7 @@ def singlepoint(
     solvation: dict | None = None,
     grad: bool = False,
     exclude: tuple = (),
+    mixer: str = "broyden1",
 ) -> Result:
     """
     GFN1/GFN2 single point: SCF on the potential to ``tol`` (the converged
@@ -887,15 +888,76 @@ def singlepoint(
             return torch.cat(parts), (p, cmat, ev, fa, fb, qo, dp, qp)
 
         x = torch.zeros(sysm.nao + (9 * nat if d is not None else 0), dtype=DT)
-        # Anderson mixing on the potential
+        # Anderson mixing on the potential (or modified Broyden, mixer="broyden")
         hist_x, hist_f = [], []
+        dfs, us, r_old, x_old = [], [], None, None
         it = 0
         for it in range(1, maxiter + 1):
             gx, aux = f_map(x)
             r = gx - x
-            if float(r.abs().max()) < tol:
+            if mixer != "broyden1" and float(r.abs().max()) < tol:
                 x = gx
                 break
+            if mixer == "broyden1":
+                # exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265 and
+                # _jacobian.py:51-120 with alpha=-0.5, damp=0.5, no line search
+                # (scf/base.py:267-292); F(x) = x - G(x), Gm = 0.5 I + C D^T
+                y = -r
+                ynorm = float(torch.linalg.norm(y))
+                if it == 1:
+                    cs, ds = [], []
+                    best = (ynorm, x.clone())
+                else:
+                    if ynorm < best[0]:
+                        best = (ynorm, x.clone())
+                    dxx, dyy = x - x_old, y - y_old
+
+                    def gm(v):
+                        out = 0.5 * v
+                        for c_, d_ in zip(cs, ds):
+                            out = out + c_ * torch.dot(d_, v)
+                        return out
+
+                    def gmt(v):
+                        out = 0.5 * v
+                        for c_, d_ in zip(cs, ds):
+                            out = out + d_ * torch.dot(c_, v)
+                        return out
+
+                    v = gmt(dxx)
+                    c_new = dxx - gm(dyy)
+                    d_new = v / torch.dot(dyy, v)
+                    cs.append(c_new)
+                    ds.append(d_new)
+                    if dx_norm < tol and ynorm < tol:
+                        break
+                if it == maxiter:
+                    x = best[1]
+                    break
+                dxv = -0.5 * y
+                for c_, d_ in zip(cs, ds):
+                    dxv = dxv - c_ * torch.dot(d_, y)
+                dx_norm = float(torch.linalg.norm(dxv))
+                x_old, y_old = x.clone(), y.clone()
+                x = x + 0.5 * dxv
+                continue
+            if mixer == "broyden":
+                if r_old is not None:
+                    dfr = r - r_old
+                    nrm = torch.linalg.norm(dfr)
+                    dfs.append(dfr / nrm)
+                    us.append(0.2 * dfr / nrm + (x - x_old) / nrm)
+                    if len(dfs) > 16:
+                        dfs.pop(0)
+                        us.pop(0)
+                x_old, r_old = x.clone(), r.clone()
+                if dfs:
+                    F, U = torch.stack(dfs, 1), torch.stack(us, 1)
+                    a = F.T @ F + 1e-4 * torch.eye(len(dfs), dtype=DT)
+                    x = x + 0.2 * r - U @ torch.linalg.solve(a, F.T @ r)
+                else:
+                    x = x + 0.2 * r
+                continue
             hist_x.append(x.clone())
             hist_f.append(r.clone())
             if len(hist_x) > 8:
