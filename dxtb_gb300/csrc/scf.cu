@@ -16,7 +16,8 @@
 
 namespace dxtb {
 
-constexpr int kScfThreads = 256;
+constexpr int kScfThreads = 256;     // CTA size for molecules sharing an SM
+constexpr int kScfBigThreads = 512;  // CTA size for large molecules on their own SM
 constexpr int kRank = 64;         // rank of the Broyden inverse-Jacobian memory
 constexpr double kDamp = 0.5;     // step damping of the root solver (defaults.DAMP)
 constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
@@ -30,7 +31,7 @@ struct MolView {
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * kScfThreads + n + 8 +
+  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * kScfBigThreads + n + 8 +
          4 * kRank + 64;
 }
 
@@ -64,7 +65,7 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.xold = q; q += N;
   w.rold = q; q += N;
   w.xbest = q; q += N;
-  w.lu = q; q += (size_t)5 * n * kScfThreads;
+  w.lu = q; q += (size_t)5 * n * kScfBigThreads;
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
   w.anderson = q; q += 4 * kRank + 64;
   w.misc = q;  // 64 + 16 nat + 2N
@@ -249,13 +250,33 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
   return block_sum(e, red);
 }
 
-__global__ void __launch_bounds__(kScfThreads, 2) k_scf(ScfArgs a) {
+// Molecules of at least kBigN orbitals among the first `nbig_max` of the
+// launch order run in a 512-thread CTA with an SM of their own; the others
+// share SMs two at a time in 256-thread CTAs. The two launches run
+// concurrently; every CTA checks which one its molecule belongs to.
+constexpr int kBigN = 128;
+
+__device__ __forceinline__ bool scf_is_big(const ScfArgs &a, int i, int nbig_max) {
+  const int m = a.order ? a.order[i] : i;
+  return i < nbig_max && (a.b.ao_off[m + 1] - a.b.ao_off[m]) >= kBigN;
+}
+
+__device__ __forceinline__ void scf_body(const ScfArgs &a, int m);
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_scf(ScfArgs a, int big, int nbig_max) {
+  const int i = blockIdx.x;
+  if (scf_is_big(a, i, nbig_max) != (big != 0)) return;
+  scf_body(a, a.order ? a.order[i] : i);
+}
+
+__device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
   __shared__ double red[32];
   __shared__ int s_flag, s_m, s_ncl;
   __shared__ double s_tri[2 * kSmemTri];
   const dxtb_batch &b = a.b;
   MolView mv;
-  mv.m = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+  mv.m = m_;
   const int m = mv.m;
   mv.a0 = b.atom_off[m];
   mv.s0 = b.shell_off[m];
@@ -580,6 +601,55 @@ using namespace dxtb;
 
 extern "C" int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat) { return ws_size_mol(n, nat); }
 
+#include <mutex>
+
+namespace dxtb {
+
+// Side stream and fork/join events per device, created once (no device
+// memory is allocated); both launches stay inside a caller's stream capture.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int sms = 0;
+};
+static std::mutex g_side_mutex;
+static SideStream g_side[64];
+
+static int32_t side_stream(SideStream **out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_side_mutex);
+  SideStream &ss = g_side[dev];
+  if (ss.s == nullptr) {
+    if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    if (cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    if (cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    if (cudaDeviceGetAttribute(&ss.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return DXTB_ERR_LAUNCH;
+  }
+  *out = &ss;
+  return DXTB_OK;
+}
+
+static int32_t launch_scf(const ScfArgs &a, int nmol, cudaStream_t st) {
+  SideStream *ss = nullptr;
+  int32_t rc = side_stream(&ss);
+  if (rc != DXTB_OK) return rc;
+  const int nbig_max = min(nmol, ss->sms / 2);
+  // big molecules on the side stream, the rest on the caller's stream
+  if (cudaEventRecord(ss->fork, st) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (cudaStreamWaitEvent(ss->s, ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (nbig_max > 0) k_scf<kScfBigThreads, 1><<<nbig_max, kScfBigThreads, 0, ss->s>>>(a, 1, nbig_max);
+  DXTB_CHECK_LAUNCH();
+  k_scf<kScfThreads, 2><<<nmol, kScfThreads, 0, st>>>(a, 0, nbig_max);
+  DXTB_CHECK_LAUNCH();
+  if (cudaEventRecord(ss->join, ss->s) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (cudaStreamWaitEvent(st, ss->join, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  return DXTB_OK;
+}
+
+}  // namespace dxtb
+
 extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                             const double *overlap, const double *h0, const double *dipole,
                             const double *quadrupole, const double *gamma, const double *hd,
@@ -630,9 +700,7 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   a.vqp = vqp;
   a.energies = energies;
   a.status = status;
-  k_scf<<<b->nmol, kScfThreads, 0, (cudaStream_t)stream>>>(a);
-  DXTB_CHECK_LAUNCH();
-  return DXTB_OK;
+  return launch_scf(a, b->nmol, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------
