@@ -31,6 +31,8 @@ import torch
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# serving slots and their side streams need more hardware queues than the default 8
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "GFN2 E+F molecules/s batched vs per-molecule at |dE|<1e-8 Eh; p50/p99 ms"
 WORKLOAD = "GFN2 E+F, 256 synthetic molecules of 10-60 atoms (H/C/N/O/F/S), packed batch"
@@ -46,6 +48,9 @@ def args():
     p.add_argument("--cpu-sample", type=int, default=12, help="molecules timed on the CPU")
     p.add_argument("--per-molecule", type=int, default=16, help="molecules on the 1-by-1 GPU path")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--serve-rate", type=float, default=2000.0,
+                   help="Poisson arrival rate of the serving leg (0: skip the leg)")
+    p.add_argument("--serve-slots", type=int, default=8)
     return p.parse_args()
 
 
@@ -302,6 +307,25 @@ def main():
             "p99_ms": 1e3 * float(np.percentile(t_e2e, 99)),
         }
 
+    # serving: the same molecules as a seeded Poisson request stream through the
+    # continuous-batching loop; latency = arrival -> energy and forces on the host
+    serving = None
+    if a.serve_rate > 0:
+        from dxtb_gb300.serving import CudaExecutor, Request, Server, latency_summary, warm_up
+
+        rng = np.random.default_rng(4000)
+        arr = np.cumsum(rng.exponential(1.0 / a.serve_rate, size=len(nums)))
+        reqs = [Request(i, "gfn2", nums[i], mols[i][1], arrival=float(arr[i])) for i in range(len(nums))]
+        ex = CudaExecutor(dev, slots=a.serve_slots)
+        warm_up(ex, a.serve_slots)
+        torch.cuda.synchronize()
+        srv = Server(ex, hbm_budget=120e9, slots=a.serve_slots, max_pack=32)
+        out = srv.serve(reqs)
+        serving = latency_summary(out)
+        serving.update({"rate_hz": a.serve_rate, "slots": a.serve_slots, "max_pack": 32,
+                        "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
+                        "hbm_budget_gb": 120.0, "status_bad": sum(1 for r in out if r.status != 0)})
+
     cpu_baseline = None
     max_de = None
     if rank == 0 and a.cpu_sample > 0:
@@ -354,7 +378,8 @@ def main():
         },
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
-        "gpu_launches": 6 * a.steps,
+        "serving": serving,
+        "gpu_launches": res.launches * a.steps,
         "clocks": clk,
     }
     print(json.dumps(line))

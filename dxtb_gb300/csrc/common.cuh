@@ -67,6 +67,21 @@ __device__ __forceinline__ double block_max(double v, double *red) {
   return r;
 }
 
+// SM count of the current device, cached per device (host side).
+inline int32_t device_sms(int *sms) {
+  static int cache[64] = {0};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
+  if (cache[dev] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      return DXTB_ERR_LAUNCH;
+    cache[dev] = v;
+  }
+  *sms = cache[dev];
+  return DXTB_OK;
+}
+
 // Molecule of a flat index given a prefix array off[0..nmol] (binary search).
 __device__ __forceinline__ int find_mol(const int64_t *off, int nmol, int64_t k) {
   int lo = 0, hi = nmol - 1;

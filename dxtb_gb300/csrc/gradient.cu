@@ -100,20 +100,14 @@ struct GPair {
   double A[3], B[3];
 };
 
-__global__ void __launch_bounds__(gWarps * 32)
-    k_grad_pairs(dxtb_batch b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
-                 const double *__restrict__ cn, const double *__restrict__ P,
-                 const double *__restrict__ W, const double *__restrict__ S,
-                 const double *__restrict__ D, const double *__restrict__ vorb,
-                 const double *__restrict__ vdp, const double *__restrict__ vqp, int64_t npairs,
-                 int multipole, double *__restrict__ dedcn, double *__restrict__ grad) {
-  extern __shared__ double smem[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *s_tab = smem + (size_t)w * (gChunk * gTab + 2 * gNComp * 36);
-  double *s_esph = s_tab + gChunk * gTab;      // [10][5][5] spherical coefficients
-  double *s_ecart = s_esph + gNComp * 36;      // [6][6][10] Cartesian coefficients
-  const int64_t k = (int64_t)blockIdx.x * gWarps + w;
-  if (k >= npairs) return;
+// One shell pair of the integral adjoint (one warp).
+__device__ __forceinline__ void grad_pair(
+    const dxtb_batch &b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
+    const double *__restrict__ cn, const double *__restrict__ P, const double *__restrict__ W,
+    const double *__restrict__ S, const double *__restrict__ D, const double *__restrict__ vorb,
+    const double *__restrict__ vdp, const double *__restrict__ vqp, int multipole,
+    double *__restrict__ dedcn, double *__restrict__ grad, int64_t k, int lane, double *s_tab,
+    double *s_esph, double *s_ecart) {
 
   GPair g;
   g.m = find_mol(b.pair_off, b.nmol, k);
@@ -329,6 +323,27 @@ __global__ void __launch_bounds__(gWarps * 32)
   }
 }
 
+__global__ void __launch_bounds__(gWarps * 32)
+    k_grad_pairs(dxtb_batch b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
+                 const double *__restrict__ cn, const double *__restrict__ P,
+                 const double *__restrict__ W, const double *__restrict__ S,
+                 const double *__restrict__ D, const double *__restrict__ vorb,
+                 const double *__restrict__ vdp, const double *__restrict__ vqp, int multipole,
+                 double *__restrict__ dedcn, double *__restrict__ grad) {
+  extern __shared__ double smem[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *s_tab = smem + (size_t)w * (gChunk * gTab + 2 * gNComp * 36);
+  double *s_esph = s_tab + gChunk * gTab;      // [10][5][5] spherical coefficients
+  double *s_ecart = s_esph + gNComp * 36;      // [6][6][10] Cartesian coefficients
+  // grid-stride over shell pairs; the exact count is read on the device
+  const int64_t npairs = b.pair_off[b.nmol];
+  for (int64_t k = (int64_t)blockIdx.x * gWarps + w; k < npairs; k += (int64_t)gridDim.x * gWarps) {
+    grad_pair(b, pf_, pi_tab, cn, P, W, S, D, vorb, vdp, vqp, multipole, dedcn, grad, k, lane, s_tab,
+              s_esph, s_ecart);
+    __syncwarp();  // the next pair reuses this warp's shared tables
+  }
+}
+
 __device__ __forceinline__ double exp_count_d(double r, double r0, double k, double *dc) {
   const double c = 1.0 / (1.0 + exp(-k * (r0 / r - 1.0)));
   *dc = -c * (1.0 - c) * k * r0 / (r * r);
@@ -340,12 +355,11 @@ __global__ void k_grad_mol(dxtb_batch b, const double *__restrict__ pf_,
                            const int32_t *__restrict__ pi_tab, const double *__restrict__ cn,
                            const double *__restrict__ mrad, const double *__restrict__ q,
                            const double *__restrict__ dp, const double *__restrict__ qp,
-                           double *__restrict__ dedcn, double *__restrict__ grad) {
+                           int multipole, double *__restrict__ dedcn, double *__restrict__ grad) {
   extern __shared__ double sm[];
   const int m = blockIdx.x;
   const int64_t a0 = b.atom_off[m], s0 = b.shell_off[m], o0 = b.ao_off[m];
   const int nat = (int)(b.atom_off[m + 1] - a0), nsh = (int)(b.shell_off[m + 1] - s0);
-  const int multipole = pi_(pi_tab, DXTB_I_SCAL + DXTB_IS_MULTIPOLE);
   const int cn_kind = pi_(pi_tab, DXTB_I_SCAL + DXTB_IS_CN_KIND);
   double *qsh = sm;              // [nsh]
   double *qat = qsh + nsh;       // [nat]
@@ -538,32 +552,28 @@ extern "C" int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f, const
       !grad)
     return DXTB_ERR_ARGS;
   cudaStream_t st = (cudaStream_t)stream;
-  int64_t npairs = 0;
-  if (cudaMemcpyAsync(&npairs, b->pair_off + b->nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, st) !=
-      cudaSuccess)
-    return DXTB_ERR_LAUNCH;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return DXTB_ERR_LAUNCH;
-  int32_t iscal[DXTB_NISCAL];
-  if (cudaMemcpy(iscal, par_i + DXTB_I_SCAL, sizeof(iscal), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return DXTB_ERR_LAUNCH;
-  const int multipole = iscal[DXTB_IS_MULTIPOLE];
-  if (multipole && (!dipole || !vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
+  // The multipole (GFN2) terms are taken iff the dipole integrals are given.
+  const int multipole = dipole != nullptr;
+  if (multipole && (!vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_grad_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gSmem);
     attr = true;
   }
-  if (npairs > 0) {
-    const int64_t blocks = (npairs + gWarps - 1) / gWarps;
+  const int64_t bound = (int64_t)b->nmol * b->max_nsh * (b->max_nsh + 1) / 2;
+  if (bound > 0) {
+    int sms = 0;
+    if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
+    const int64_t blocks = min((bound + gWarps - 1) / gWarps, (int64_t)sms * 16);
     k_grad_pairs<<<(unsigned)blocks, gWarps * 32, gSmem, st>>>(*b, par_f, par_i, cn, density, wdensity,
-                                                               overlap, dipole, vorb, vdp, vqp, npairs,
-                                                               multipole, dedcn, grad);
+                                                               overlap, dipole, vorb, vdp, vqp, multipole,
+                                                               dedcn, grad);
     DXTB_CHECK_LAUNCH();
   }
   const size_t smem = sizeof(double) * (size_t)(b->max_nsh + 3 * b->max_nat + 8);
   if (smem > 200 * 1024) return DXTB_ERR_TOO_LARGE;
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_grad_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_grad_mol<<<b->nmol, 128, smem, st>>>(*b, par_f, par_i, cn, mrad, q, dp, qp, dedcn, grad);
+  k_grad_mol<<<b->nmol, 128, smem, st>>>(*b, par_f, par_i, cn, mrad, q, dp, qp, multipole, dedcn, grad);
   DXTB_CHECK_LAUNCH();
   return DXTB_OK;
 }

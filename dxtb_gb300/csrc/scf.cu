@@ -1,8 +1,8 @@
 // Persistent self-consistent-field kernel: one CTA per molecule runs the
 // whole SCF of that molecule (orthogonaliser, Fock build, generalized
 // eigensolve, Fermi occupations, density, Mulliken charges and atomic
-// multipoles, potentials, Anderson mixing) with a per-molecule convergence
-// test and iteration cap. No host synchronisation inside the loop.
+// multipoles, potentials, limited-memory Broyden root solve) with a
+// per-molecule convergence test and iteration cap. No host synchronisation inside the loop.
 //
 // Reference path (src/dxtb/_src): scf/iterator.py:51-195, scf/pure/
 // conversions.py:106-366 (charges <-> potential <-> Fock <-> density),
@@ -37,7 +37,7 @@ __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
 
 struct Ws {
   double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
-  double *vsh_tmp, *lu, *anderson, *xold, *rold, *xbest;
+  double *vsh_tmp, *lu, *sdot, *xold, *rold, *xbest;
   int *cl;
 };
 
@@ -67,7 +67,7 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.xbest = q; q += N;
   w.lu = q; q += (size_t)5 * n * kScfBigThreads;
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
-  w.anderson = q; q += 4 * kRank + 64;
+  w.sdot = q; q += 4 * kRank + 64;
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
@@ -441,7 +441,7 @@ __device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
     // alpha = -0.5, damp = 0.5, line_search = False, scf/base.py:267-292);
     // stop when |dx|_2 < x_tol and |F|_2 < f_tol. ----
     {
-      double *sdot = w.anderson;                 // [kRank] dot products
+      double *sdot = w.sdot;                     // [kRank] dot products
       double *sdot2 = sdot + kRank;              // [kRank]
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
       const int nw = (int)(blockDim.x >> 5);
@@ -605,46 +605,67 @@ extern "C" int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat) { return ws_si
 
 namespace dxtb {
 
-// Side stream and fork/join events per device, created once (no device
-// memory is allocated); both launches stay inside a caller's stream capture.
+// Side stream and fork/join events per (device, caller stream), created once
+// (no device memory is allocated); both launches stay inside a caller's
+// stream capture. Callers on different streams (the serving loop's slots)
+// get different side streams, so their large-molecule kernels overlap.
 struct SideStream {
+  cudaStream_t caller = nullptr;
   cudaStream_t s = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
-  int sms = 0;
+  bool used = false;
 };
+constexpr int kSidePerDev = 32;
 static std::mutex g_side_mutex;
-static SideStream g_side[64];
+static SideStream g_side[64][kSidePerDev];
 
-static int32_t side_stream(SideStream **out) {
+// nullptr (and DXTB_OK) when the table is full: both launches then go to
+// the caller's stream, one after the other.
+static int32_t side_stream(cudaStream_t caller, SideStream **out) {
+  *out = nullptr;
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
   std::lock_guard<std::mutex> lock(g_side_mutex);
-  SideStream &ss = g_side[dev];
-  if (ss.s == nullptr) {
-    if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess) return DXTB_ERR_LAUNCH;
-    if (cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
-    if (cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
-    if (cudaDeviceGetAttribute(&ss.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      return DXTB_ERR_LAUNCH;
+  SideStream *slot = nullptr;
+  for (int i = 0; i < kSidePerDev; ++i) {
+    SideStream &ss = g_side[dev][i];
+    if (ss.used && ss.caller == caller) {
+      *out = &ss;
+      return DXTB_OK;
+    }
+    if (!ss.used && slot == nullptr) slot = &ss;
   }
-  *out = &ss;
+  if (slot == nullptr) return DXTB_OK;
+  if (cudaStreamCreateWithFlags(&slot->s, cudaStreamNonBlocking) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (cudaEventCreateWithFlags(&slot->fork, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (cudaEventCreateWithFlags(&slot->join, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  slot->caller = caller;
+  slot->used = true;
+  *out = slot;
   return DXTB_OK;
 }
 
 static int32_t launch_scf(const ScfArgs &a, int nmol, cudaStream_t st) {
   SideStream *ss = nullptr;
-  int32_t rc = side_stream(&ss);
+  int32_t rc = side_stream(st, &ss);
   if (rc != DXTB_OK) return rc;
-  const int nbig_max = min(nmol, ss->sms / 2);
+  int sms = 0;
+  if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
+  const int nbig_max = min(nmol, sms / 2);
   // big molecules on the side stream, the rest on the caller's stream
-  if (cudaEventRecord(ss->fork, st) != cudaSuccess) return DXTB_ERR_LAUNCH;
-  if (cudaStreamWaitEvent(ss->s, ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
-  if (nbig_max > 0) k_scf<kScfBigThreads, 1><<<nbig_max, kScfBigThreads, 0, ss->s>>>(a, 1, nbig_max);
+  cudaStream_t sb = ss ? ss->s : st;
+  if (ss) {
+    if (cudaEventRecord(ss->fork, st) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    if (cudaStreamWaitEvent(ss->s, ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  }
+  if (nbig_max > 0) k_scf<kScfBigThreads, 1><<<nbig_max, kScfBigThreads, 0, sb>>>(a, 1, nbig_max);
   DXTB_CHECK_LAUNCH();
   k_scf<kScfThreads, 2><<<nmol, kScfThreads, 0, st>>>(a, 0, nbig_max);
   DXTB_CHECK_LAUNCH();
-  if (cudaEventRecord(ss->join, ss->s) != cudaSuccess) return DXTB_ERR_LAUNCH;
-  if (cudaStreamWaitEvent(st, ss->join, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (ss) {
+    if (cudaEventRecord(ss->join, ss->s) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    if (cudaStreamWaitEvent(st, ss->join, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  }
   return DXTB_OK;
 }
 

@@ -124,6 +124,7 @@ class PackedBatch:
             "n0": dev(np.concatenate(n0), F64),
             "nel": dev(np.array(nel, dtype=np.float64), F64),
             "order": dev(np.argsort(-nao, kind="stable").astype(np.int32), torch.int32),
+            "atom_mol": dev(np.repeat(np.arange(self.nmol), nat), torch.int64),
             "par_f": dev(tables.f64, F64),
             "par_i": dev(tables.i32, torch.int32),
         }
@@ -170,14 +171,32 @@ class Result:
     status: torch.Tensor           # [nmol] int32
     gradient: torch.Tensor | None  # [natoms, 3] packed
     state: dict
+    launches: int = 0              # kernels of the library launched by this call
 
 
-def _seg_sum(values: torch.Tensor, off: np.ndarray, nmol: int) -> torch.Tensor:
-    idx = torch.repeat_interleave(
-        torch.arange(nmol, device=values.device),
-        torch.as_tensor(np.diff(off), device=values.device),
-    )
-    return torch.zeros(nmol, dtype=values.dtype, device=values.device).index_add_(0, idx, values)
+def _seg_sum(values: torch.Tensor, seg: torch.Tensor, nmol: int) -> torch.Tensor:
+    """Per-molecule sums of a packed per-atom vector (seg: molecule of each atom, on the device)."""
+    return torch.zeros(nmol, dtype=values.dtype, device=values.device).index_add_(0, seg, values)
+
+
+GB_KERNELS = {"p16": 0, "still": 1}
+
+
+def gb_args(gb: dict) -> tuple:
+    """
+    (epsilon, kernel, alpb, born_scale, born_offset) of a solvation dict with
+    the arguments of ``GeneralizedBorn`` (solvation/alpb.py:213-245):
+    ``epsilon`` (dielectric constant), ``alpb`` (default True), ``kernel``
+    ("p16" default, or "still"), ``born_scale`` (1.0), ``born_offset`` (0.0).
+    """
+    eps = float(gb["epsilon"])
+    if not eps > 0.0:
+        raise ValueError("dielectric constant must be positive")
+    kernel = gb.get("kernel", "p16")
+    if kernel not in GB_KERNELS:
+        raise ValueError(f"unknown Born kernel {kernel!r}")
+    return (eps, GB_KERNELS[kernel], 1 if gb.get("alpb", True) else 0,
+            float(gb.get("born_scale", 1.0)), float(gb.get("born_offset", 0.0)))
 
 
 def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float = 1e-10,
@@ -220,10 +239,12 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
     cn = buf("cn", na)
     mark("geometry", 0)
     _lib.check(L.dxtb_coordination_number(b, pf, pi, tb.cn_kind, cn.data_ptr(), st), "coordination number")
+    launches = 1
     cn_mp = cn
     if mp and tb.cn_kind != 1:
         cn_mp = buf("cn_mp", na)
         _lib.check(L.dxtb_coordination_number(b, pf, pi, 1, cn_mp.data_ptr(), st), "coordination number")
+        launches += 1
     gamma, hd = buf("gamma", g2), buf("hd", ns if tb.es3_shell else na)
     erep = buf("erep", na)
     mrad = buf("mrad", na) if mp else None
@@ -236,16 +257,17 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                                  erep.data_ptr(), st),
         "interaction cache",
     )
+    launches += 1
     gbm = None
     if gb is not None:
+        ga = gb_args(gb)
         gbm = buf("gb", n2)
-        born = buf("born", na)
         _lib.check(
-            L.dxtb_born_matrix(b, pf, pi, float(gb["epsilon"]), float(gb.get("born_scale", 1.0)),
-                               float(gb.get("born_offset", 0.0)), float(gb.get("kernel", 0)),
-                               born.data_ptr(), gbm.data_ptr(), buf("psi", na).data_ptr(), st),
+            L.dxtb_born_matrix(b, pf, pi, *ga, buf("born", na).data_ptr(), buf("psi", na).data_ptr(),
+                               gbm.data_ptr(), st),
             "generalized Born",
         )
+        launches += 1
     S, H = buf("S", nm), buf("H", nm)
     D = buf("D", 3 * nm) if mp else None
     Q = buf("Q", 6 * nm) if mp else None
@@ -253,6 +275,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
     mark("integrals", 0)
     _lib.check(L.dxtb_multipole_h0(b, pf, pi, cn.data_ptr(), S.data_ptr(), H.data_ptr(),
                                    _lib.ptr(D), _lib.ptr(Q), st), "multipole integrals")
+    launches += 1
     mark("integrals", 1)
     P, Cm = buf("P", nm), buf("C", nm)
     W = buf("W", nm) if forces else None
@@ -278,9 +301,10 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                    en.data_ptr(), status.data_ptr(), st),
         "SCF",
     )
+    launches += 2  # large- and small-molecule SCF kernels
     mark("scf", 1)
     e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
-    e_rep = _seg_sum(erep[:na], pb.atom_off, pb.nmol)
+    e_rep = _seg_sum(erep[:na], pb.t["atom_mol"], pb.nmol)
     grad = None
     if forces:
         grad = buf("grad", 3 * na)
@@ -298,15 +322,15 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                             dedcn.data_ptr(), _lib.ptr(dedcn_mp), grad.data_ptr(), st),
             "gradient",
         )
+        launches += 2
         mark("gradient", 1)
         if gb is not None:
             _lib.check(
-                L.dxtb_born_gradient(b, pf, pi, q.data_ptr(), s["born"].data_ptr(), s["psi"].data_ptr(),
-                                     gbm.data_ptr(), None, None, float(gb["epsilon"]),
-                                     float(gb.get("born_scale", 1.0)), float(gb.get("born_offset", 0.0)),
-                                     float(gb.get("kernel", 0)), grad.data_ptr(), None, st),
+                L.dxtb_born_gradient(b, pf, pi, *ga, q.data_ptr(), s["born"].data_ptr(),
+                                     s["psi"].data_ptr(), grad.data_ptr(), st),
                 "generalized Born gradient",
             )
+            launches += 1
         grad = grad[: 3 * na].view(na, 3)
     energy = e4[:, 0] + e4[:, 1] + e_rep
-    return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], status[: pb.nmol], grad, s)
+    return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], status[: pb.nmol], grad, s, launches)

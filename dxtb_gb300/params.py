@@ -213,6 +213,12 @@ class Tables:
         self.multipole = bool(mp)
         self.es3_shell = es3_shell
         self.cn_kind = 0 if xtb.get("cn", "exp") == "exp" else 1
+        # shells and spherical orbitals per element (0 for elements without parameters)
+        self.el_nsh = np.zeros(maxz, dtype=np.int64)
+        self.el_nao = np.zeros(maxz, dtype=np.int64)
+        for z, ang in self.el_angular.items():
+            self.el_nsh[z] = len(ang)
+            self.el_nao[z] = sum(2 * l + 1 for l in ang)
 
     def check_elements(self, numbers) -> None:
         z = set(int(v) for v in np.asarray(numbers).ravel() if v > 0)

@@ -1,0 +1,394 @@
+"""
+Continuous-batching request loop for GFN1/GFN2 single points on one GPU.
+
+Requests (energy, optionally forces) of any size and either method arrive
+over time. The loop keeps up to ``slots`` packs in flight, one CUDA stream
+per slot. Whenever a slot frees up, the queued requests are admitted in
+arrival order into a new pack of one method. The pack is limited to
+``max_pack`` molecules and to the HBM still free under the budget. Each
+pack is one packed batch pushed through the device pipeline (geometry ->
+integrals -> persistent SCF -> adjoint gradient) on its slot's stream. Its
+basis, integral and density state stays device-resident until the host
+has its results. Packs on different streams run concurrently: a pack's
+SCF kernel holds one SM (or half of one) per molecule, so the other
+packs' molecules run on the SMs left free. Each molecule's SCF runs in
+its own CTA with a fixed reduction order, so a result does not depend on
+the pack it was admitted in.
+
+The reference has no serving loop: it evaluates one ``Calculator`` call
+at a time (``calculators/types/energy.py:78-414``). This module adds
+admission and overlap around that call. Each request's numerics are the
+batched single point of ``engine.run``.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+METHODS = ("gfn1", "gfn2")
+
+
+@dataclass
+class Request:
+    rid: int
+    method: str                    # "gfn1" or "gfn2"
+    numbers: np.ndarray            # (nat,) atomic numbers
+    positions: np.ndarray          # (nat, 3) Bohr
+    chrg: float = 0.0
+    spin: int | None = None
+    forces: bool = True
+    arrival: float = 0.0           # seconds on the server clock
+
+
+@dataclass
+class Response:
+    rid: int
+    energy: float
+    forces: np.ndarray | None      # -dE/dR (nat, 3)
+    iterations: int
+    status: int                    # 0 ok, else a DXTB_ERR_* code
+    arrival: float
+    admitted: float
+    done: float
+    pack: int
+    pack_size: int
+    error: str | None = None
+
+    @property
+    def latency_ms(self) -> float:
+        return 1e3 * (self.done - self.arrival)
+
+
+@dataclass
+class _Pack:
+    pid: int
+    slot: int
+    requests: list
+    nbytes: int
+    admitted: float
+    handle: object = None
+
+
+@dataclass
+class Stats:
+    requests: int = 0
+    packs: int = 0
+    max_inflight: int = 0
+    max_bytes: int = 0
+    rejected: int = 0
+    pack_sizes: list = field(default_factory=list)
+
+
+class Server:
+    """
+    Admission and completion loop. ``executor`` does the device work; it
+    provides ``nbytes(req)``, ``launch(reqs, slot) -> handle``,
+    ``ready(handle) -> bool`` and ``collect(handle) -> list of (energy,
+    forces, iterations, status)``. Packs are admitted FIFO: the oldest
+    queued request fixes the pack's method, and younger requests of that
+    method join while they fit.
+    """
+
+    def __init__(self, executor, *, hbm_budget: float = 120e9, slots: int = 8, max_pack: int = 32,
+                 clock=time.perf_counter):
+        if slots < 1 or max_pack < 1:
+            raise ValueError("slots and max_pack must be positive")
+        self.ex = executor
+        self.budget = int(hbm_budget)
+        self.slots = slots
+        self.max_pack = max_pack
+        self.clock = clock
+        self.t0 = clock()
+        self.queue: deque = deque()
+        self.free_slots = list(range(slots))
+        self.inflight: list[_Pack] = []
+        self.used = 0
+        self.stats = Stats()
+        self._pid = 0
+
+    def now(self) -> float:
+        return self.clock() - self.t0
+
+    def submit(self, req: Request) -> None:
+        if req.method not in METHODS:
+            raise ValueError(f"unknown method {req.method!r}")
+        self.queue.append(req)
+        self.stats.requests += 1
+
+    @property
+    def idle(self) -> bool:
+        return not self.queue and not self.inflight
+
+    def _reap(self) -> list[Response]:
+        out = []
+        keep = []
+        for pk in self.inflight:
+            if not self.ex.ready(pk.handle):
+                keep.append(pk)
+                continue
+            res = self.ex.collect(pk.handle)
+            t = self.now()
+            for r, (e, f, it, st) in zip(pk.requests, res):
+                out.append(Response(r.rid, float(e), f, int(it), int(st), r.arrival, pk.admitted, t,
+                                    pk.pid, len(pk.requests)))
+            self.used -= pk.nbytes
+            self.free_slots.append(pk.slot)
+            pk.handle = None
+        self.inflight = keep
+        return out
+
+    def _admit(self) -> list[Response]:
+        out = []
+        while self.free_slots and self.queue:
+            head = self.queue[0]
+            free = self.budget - self.used
+            nb = self.ex.nbytes(head)
+            if nb > self.budget:
+                # can never fit: answer it with an error instead of blocking the queue
+                self.queue.popleft()
+                t = self.now()
+                out.append(Response(head.rid, math.nan, None, 0, 7, head.arrival, t, t, -1, 0,
+                                    error="request exceeds the HBM budget"))
+                self.stats.rejected += 1
+                continue
+            if nb > free:
+                break  # wait for memory: in-flight packs will release it
+            take, rest, tot = [], deque(), 0
+            while self.queue:
+                r = self.queue.popleft()
+                if len(take) < self.max_pack and r.method == head.method:
+                    b = nb if r is head else self.ex.nbytes(r)
+                    if tot + b <= free:
+                        take.append(r)
+                        tot += b
+                        continue
+                rest.append(r)
+            self.queue = rest
+            slot = self.free_slots.pop(0)
+            pk = _Pack(self._pid, slot, take, tot, self.now())
+            self._pid += 1
+            pk.handle = self.ex.launch(take, slot)
+            self.inflight.append(pk)
+            self.used += tot
+            self.stats.packs += 1
+            self.stats.pack_sizes.append(len(take))
+            self.stats.max_inflight = max(self.stats.max_inflight, len(self.inflight))
+            self.stats.max_bytes = max(self.stats.max_bytes, self.used)
+        return out
+
+    def pump(self) -> list[Response]:
+        """Reap finished packs, then admit queued requests into free slots."""
+        out = self._reap()
+        out += self._admit()
+        return out
+
+    def serve(self, requests: list[Request], *, poll: float = 5e-5) -> list[Response]:
+        """
+        Replay ``requests`` (sorted by ``arrival``) against the server clock:
+        each is submitted when its arrival time has passed, and the loop
+        pumps until every request has a response.
+        """
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        self.t0 = self.clock()
+        out: list[Response] = []
+        i = 0
+        while i < len(reqs) or not self.idle:
+            now = self.now()
+            while i < len(reqs) and reqs[i].arrival <= now:
+                self.submit(reqs[i])
+                i += 1
+            got = self.pump()
+            out += got
+            if not got:
+                nxt = reqs[i].arrival - self.now() if i < len(reqs) else poll
+                time.sleep(max(0.0, min(poll, nxt)))
+        return out
+
+
+def latency_summary(responses: list[Response]) -> dict:
+    """p50/p99 latency (arrival -> result on the host) and throughput."""
+    ok = [r for r in responses if r.status == 0 and r.error is None]
+    lat = np.array([r.latency_ms for r in ok]) if ok else np.zeros(1)
+    span = (max(r.done for r in ok) - min(r.arrival for r in ok)) if ok else 0.0
+    return {
+        "requests": len(responses),
+        "ok": len(ok),
+        "p50_ms": float(np.percentile(lat, 50)),
+        "p99_ms": float(np.percentile(lat, 99)),
+        "max_ms": float(lat.max()),
+        "mol_per_s": len(ok) / span if span > 0 else 0.0,
+        "span_s": span,
+    }
+
+
+def poisson_requests(count: int, rate: float, seed: int, *, methods=("gfn1", "gfn2"),
+                     nat_range=(8, 300), log_uniform: bool = True, forces: bool = True) -> list[Request]:
+    """
+    Seeded Poisson request stream. Inter-arrival times are
+    ``rng.exponential(1/rate)``. Methods are drawn uniformly from
+    ``methods``, and atom counts log-uniformly (or uniformly) in
+    ``nat_range``. Molecule i is ``random_molecule`` with seed
+    4000 + i (the serving configuration's seed block).
+    """
+    from .workloads import random_molecule
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    lo, hi = nat_range
+    for i in range(count):
+        t += rng.exponential(1.0 / rate)
+        m = methods[int(rng.integers(len(methods)))]
+        if log_uniform:
+            nat = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        else:
+            nat = int(rng.integers(lo, hi + 1))
+        z, x = random_molecule(4000 + i, nat)
+        out.append(Request(i, m, z, x, forces=forces, arrival=t))
+    return out
+
+
+class CudaExecutor:
+    """
+    Device work of the server: one packed batch per pack on the slot's CUDA
+    stream, results copied into pinned host buffers and fenced by an event.
+    """
+
+    def __init__(self, device="cuda", *, slots: int = 8, etemp: float = 300.0, maxiter: int = 250,
+                 tol: float = 1e-10):
+        import torch
+
+        from . import _lib
+        from .params import Tables
+
+        _lib.lib()  # fails loudly without the CUDA library
+        self.torch = torch
+        self.device = torch.device(device)
+        self.tables = {m: Tables(m) for m in METHODS}
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.opts = dict(etemp=etemp, maxiter=maxiter, tol=tol)
+        self._ws = {}
+
+    def _sizes(self, req: Request) -> tuple[int, int, int]:
+        tb = self.tables[req.method]
+        z = np.asarray(req.numbers, dtype=np.int64)
+        tb.check_elements(z)
+        return int(tb.el_nao[z].sum()), len(z), int(tb.el_nsh[z].sum())
+
+    def nbytes(self, req: Request) -> int:
+        """Device bytes of one request's state (integrals, caches, SCF workspace, outputs)."""
+        from . import _lib
+
+        n, nat, nsh = self._sizes(req)
+        key = (n, nat)
+        if key not in self._ws:
+            self._ws[key] = int(_lib.lib().dxtb_scf_workspace_mol(n, nat))
+        mp = req.method == "gfn2"
+        mats = (5 + (9 if mp else 0)) * n * n          # S H P C W (+ D Q)
+        caches = nsh * nsh + (18 * nat * nat if mp else 0)
+        vecs = 16 * n + 40 * nat
+        return 8 * (mats + caches + vecs + self._ws[key]) + 4096
+
+    def launch(self, reqs: list[Request], slot: int):
+        torch = self.torch
+        from .engine import PackedBatch, run
+
+        s = self.streams[slot]
+        method = reqs[0].method
+        with torch.cuda.stream(s):
+            pb = PackedBatch(self.tables[method], [r.numbers for r in reqs], [r.positions for r in reqs],
+                             device=self.device, charges=[r.chrg for r in reqs],
+                             spins=[r.spin for r in reqs])
+            forces = any(r.forces for r in reqs)
+            res = run(pb, forces=forces, **self.opts)
+            nm = pb.nmol
+            host = {
+                "energy": torch.empty(nm, dtype=torch.float64, pin_memory=True),
+                "iters": torch.empty(nm, dtype=torch.float64, pin_memory=True),
+                "status": torch.empty(nm, dtype=torch.int32, pin_memory=True),
+            }
+            host["energy"].copy_(res.energy, non_blocking=True)
+            host["iters"].copy_(res.iterations, non_blocking=True)
+            host["status"].copy_(res.status, non_blocking=True)
+            if forces:
+                host["grad"] = torch.empty(res.gradient.shape, dtype=torch.float64, pin_memory=True)
+                host["grad"].copy_(res.gradient, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(s)
+        return {"pb": pb, "res": res, "host": host, "event": ev, "reqs": reqs}
+
+    def ready(self, h) -> bool:
+        return h["event"].query()
+
+    def collect(self, h) -> list:
+        host = h["host"]
+        pb = h["pb"]
+        e = host["energy"].numpy()
+        it = host["iters"].numpy()
+        st = host["status"].numpy()
+        g = host["grad"].numpy() if "grad" in host else None
+        out = []
+        for i, r in enumerate(h["reqs"]):
+            f = None
+            if g is not None and r.forces:
+                a0, a1 = int(pb.atom_off[i]), int(pb.atom_off[i + 1])
+                f = -g[a0:a1].copy()
+            out.append((e[i], f, it[i], st[i]))
+        h.clear()  # release the pack's device state
+        return out
+
+
+def warm_up(executor, slots: int, seed: int = 99) -> None:
+    """Load the kernels and create every slot's streams before timing."""
+    from .workloads import random_molecule
+
+    srv = Server(executor, slots=slots, max_pack=1)
+    for i in range(slots):
+        z, x = random_molecule(seed + i, 8)
+        srv.submit(Request(i, METHODS[i % 2], z, x))
+    while not srv.idle:
+        srv.pump()
+
+
+def main(argv=None) -> None:
+    """Serving run on a seeded Poisson stream; prints one JSON line."""
+    import argparse
+    import json
+    import os
+
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    p = argparse.ArgumentParser(description=main.__doc__)
+    p.add_argument("--requests", type=int, default=200)
+    p.add_argument("--rate", type=float, default=2000.0, help="mean arrivals per second")
+    p.add_argument("--nat", type=int, nargs=2, default=(8, 300))
+    p.add_argument("--methods", default="gfn1,gfn2")
+    p.add_argument("--seed", type=int, default=4)
+    p.add_argument("--slots", type=int, default=8)
+    p.add_argument("--max-pack", type=int, default=32)
+    p.add_argument("--budget-gb", type=float, default=120.0)
+    a = p.parse_args(argv)
+    methods = tuple(a.methods.split(","))
+    reqs = poisson_requests(a.requests, a.rate, a.seed, methods=methods, nat_range=tuple(a.nat))
+    ex = CudaExecutor(slots=a.slots)
+    warm_up(ex, a.slots)
+    srv = Server(ex, hbm_budget=a.budget_gb * 1e9, slots=a.slots, max_pack=a.max_pack)
+    out = srv.serve(reqs)
+    s = latency_summary(out)
+    s.update({
+        "rate_hz": a.rate, "nat_range": list(a.nat), "methods": list(methods), "seed": a.seed,
+        "slots": a.slots, "max_pack": a.max_pack, "budget_gb": a.budget_gb,
+        "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
+        "max_bytes_gb": srv.stats.max_bytes / 1e9,
+        "iterations_max": max(r.iterations for r in out),
+        "status_bad": sum(1 for r in out if r.status != 0),
+    })
+    print(json.dumps(s))
+
+
+if __name__ == "__main__":
+    main()

@@ -53,7 +53,21 @@ def build_geometry(rng, heavy: list[int], nh: int) -> tuple[np.ndarray, np.ndarr
 
 
 def random_molecule(seed: int, nat: int) -> tuple[np.ndarray, np.ndarray]:
-    """Neutral closed-shell molecule with ``nat`` (+-1) atoms of the mix."""
+    """
+    Neutral closed-shell molecule with ``nat`` (+-1) atoms of the mix. A draw
+    whose hydrogens cannot all be placed (e.g. one heavy atom with eleven H)
+    is redrawn with seed ``seed + 10_000_000 * k``, k = 1, 2, ...; every
+    molecule that places at its own seed is unaffected by this rule.
+    """
+    for k in range(16):
+        try:
+            return _draw(seed + 10_000_000 * k, nat)
+        except RuntimeError:
+            continue
+    raise RuntimeError(f"no placeable molecule of {nat} atoms from seed {seed}")
+
+
+def _draw(seed: int, nat: int) -> tuple[np.ndarray, np.ndarray]:
     rng = np.random.default_rng(seed)
     z = rng.choice(ELEMENTS, size=nat, p=WEIGHTS)
     heavy = [int(v) for v in z if v != 1]
