@@ -101,9 +101,15 @@ class Calculator:
         self.opts = dict(opts or {})
         self.solvation = solvation
         if interaction is not None:
+            from .solvation import GeneralizedBorn
+
             for it in interaction if isinstance(interaction, (list, tuple)) else [interaction]:
-                if isinstance(it, dict) and "epsilon" in it:
+                if isinstance(it, GeneralizedBorn):
+                    self.solvation = it.as_dict()
+                elif isinstance(it, dict) and "epsilon" in it:
                     self.solvation = it
+                else:
+                    raise NotImplementedError(f"interaction {type(it).__name__} is not on the GB300 path")
         excl = set(self.opts.get("exclude", []))
         if not {"disp", "d4sc"}.issubset(excl) or (self.method == "gfn1" and "hal" not in excl):
             warnings.warn(
@@ -117,6 +123,10 @@ class Calculator:
         self._mols = [n[n > 0] for n in nums]
         for n in self._mols:
             self.tables.check_elements(n)
+            if self.solvation is not None:
+                from .data import radii
+
+                radii.lookup(radii.VDW_D3, n, "van-der-Waals")
         self._pb: engine.PackedBatch | None = None
         self._pb_key = None
         self._state: dict = {}

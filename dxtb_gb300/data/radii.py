@@ -15,7 +15,13 @@ values below are the published tables those names refer to:
     ``atomicrad`` table of tblite), in Ångström.
 ``VDW_D3``
     Atomic van-der-Waals radii of DFT-D3 (used for the Born radii of the
-    generalized-Born solvation model), in Ångström.
+    generalized-Born solvation model), in Ångström. H, B, N, O, F, Na, Al,
+    Si and Cl are pinned by the tblite descreening integrals psi of
+    MB16_43_01 and SiH4 in dxtb's ``test/test_solvation/samples.py``. A
+    least-squares fit of all eight MB16_43_01 radii to its 16 psi values
+    returns them at the 5-digit table values, with a relative residual of
+    2e-15 (``tests/golden/fit_vdw_radii.py``). C and S are the published
+    table values; no fixture contains them.
 
 Only elements whose values are either pinned by the dxtb test fixtures
 (``test/test_hamiltonian/h0.npz``, computed with tblite 0.3.0) or required
@@ -50,7 +56,8 @@ _ATOMIC_RADII_AA = {
     16: 1.04, 17: 1.00, 18: 1.01,
 }
 _VDW_D3_AA = {
-    1: 1.09155, 6: 1.45515, 7: 1.31125, 8: 1.24085, 9: 1.14980, 16: 1.66330,
+    1: 1.09155, 5: 1.60800, 6: 1.45515, 7: 1.31125, 8: 1.24085, 9: 1.14980,
+    11: 1.85410, 13: 2.00530, 14: 1.89585, 16: 1.66330, 17: 1.55230,
 }
 
 MAXZ = 86

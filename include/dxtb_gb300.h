@@ -202,9 +202,10 @@ int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
  * launch, one CTA per molecule (scf/iterator.py:51-144 with scf/pure/*,
  * wavefunction/filling.py:428-742, exlibs/xitorch symeig): Fock build,
  * generalized eigensolve, Fermi occupations at kT, density, Mulliken
- * charges and multipole moments, potentials, Anderson mixing of the
- * potential; per-molecule convergence (max |G(x) - x| < tol) and iteration
- * cap. order: [nmol] launch order (largest first) or null. Inputs are the
+ * charges and multipole moments, potentials, and the limited-memory
+ * Broyden root solve of x - G(x) on the potential (xitorch broyden1,
+ * exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265); per-molecule
+ * convergence |dx|_2 < tol and |x - G(x)|_2 < tol, iteration cap. order: [nmol] launch order (largest first) or null. Inputs are the
  * integrals and caches of the calls above, n0 [naos] reference occupation,
  * nel [nmol][2] alpha/beta electrons, gb_mat [nat2] or null. Outputs:
  * density [mat], wdensity [mat] (energy-weighted, may be null), coeff [mat]
@@ -228,7 +229,9 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
 /* Nuclear gradient dE/dR [natoms][3] at the converged SCF (analytic
  * adjoint; the reference differentiates with autograd through
  * calculators/types/autograd.py:84-196 and scf/implicit/fixed_point.py).
- * Accumulates into grad (caller zeroes it). */
+ * Accumulates into grad (caller zeroes it). The GFN2 multipole terms are
+ * included iff dipole is non-null; then mrad, dp, qp, vdp and vqp are
+ * required. No host synchronisation (capturable in a CUDA graph). */
 int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
                       const int32_t *par_i, const double *cn,
                       const double *cn_mp, const double *mrad,
@@ -239,6 +242,33 @@ int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
                       const double *reserved0, const double *reserved1,
                       double *dedcn, double *dedcn_mp, double *grad,
                       void *stream);
+
+/* Generalized-Born / ALPB solvation cache (one CTA per molecule): Born
+ * radii by the Onufriev-Bashford-Case descreening integral (solvation/
+ * born.py:60-239, obc = 1.0/0.8/4.85, descreening 0.8, cutoff 66 Bohr,
+ * D3 van-der-Waals radii from par_f) and the matrix
+ * A_ij = keps f(R_ij, B_i B_j) [+ keps alpbet adet] of solvation/alpb.py:
+ * 94-184, 227-321 with alpbet = 0.571412 / epsilon (alpb != 0) or 0,
+ * keps = (1/epsilon - 1) / (1 + alpbet); kernel 0 = P16, 1 = Still.
+ * Outputs: born [natoms], psi [natoms] (kept for the gradient), gb_mat
+ * [nat2] for dxtb_scf. The reference keeps the same matrix in
+ * GeneralizedBornCache.mat. */
+int32_t dxtb_born_matrix(const dxtb_batch *b, const double *par_f,
+                         const int32_t *par_i, double epsilon, int32_t kernel,
+                         int32_t alpb, double born_scale, double born_offset,
+                         double *born, double *psi, double *gb_mat, void *stream);
+
+/* Nuclear gradient of E_GB = 1/2 q_at^T A q_at at the converged orbital
+ * charges q [naos] (atom sums taken here), with born and psi from
+ * dxtb_born_matrix: explicit distance dependence of the kernel, the Born
+ * radii through psi, and the ALPB shape term (zero for neutral molecules).
+ * Accumulates into grad [natoms][3]. The reference obtains it by autograd
+ * through GeneralizedBorn.get_cache. */
+int32_t dxtb_born_gradient(const dxtb_batch *b, const double *par_f,
+                           const int32_t *par_i, double epsilon, int32_t kernel,
+                           int32_t alpb, double born_scale, double born_offset,
+                           const double *q, const double *born, const double *psi,
+                           double *grad, void *stream);
 
 /* SCF without any device allocation. No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc (code running under someone

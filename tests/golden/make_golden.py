@@ -68,6 +68,25 @@ def _ref_vector(src: str) -> np.ndarray:
     )
 
 
+def _refs_dict(src: str, var: str = "refs") -> dict[str, dict[str, np.ndarray]]:
+    """The literal ``{name: {key: torch.tensor([...]), ...}}`` dict ``var`` of a samples file."""
+    tree = ast.parse(src)
+    for node in ast.walk(tree):
+        tgt = getattr(node, "target", None) or (getattr(node, "targets", [None]) or [None])[0]
+        if isinstance(node, (ast.Assign, ast.AnnAssign)) and isinstance(tgt, ast.Name) and tgt.id == var:
+            out = {}
+            for kn, vn in zip(node.value.keys, node.value.values):
+                rec = {}
+                for kk, vv in zip(vn.keys, vn.values):
+                    if isinstance(vv, ast.Call) and vv.args:
+                        arr = np.array(ast.literal_eval(vv.args[0]), dtype=np.float64)
+                        if arr.size:
+                            rec[kk.value] = arr
+                out[kn.value] = rec
+            return out
+    raise KeyError(var)
+
+
 def main(ref_root: str) -> None:
     root = Path(ref_root)
     test = root / "test"
@@ -108,6 +127,19 @@ def main(ref_root: str) -> None:
         for name, arr in _tensor_literals(aes, func).items():
             g[f"aes2_{func}/{name}"] = arr
     src["aes2_*"] = "test/test_coulomb/test_aes2.py (LiH, inline tensors)"
+    # generalized Born / ALPB solvation (tblite reference values)
+    solv = _refs_dict((test / "test_solvation" / "samples.py").read_text())
+    for m in ("MB16_43_01", "SiH4"):
+        for key, arr in solv[m].items():
+            g[f"solv/{m}/{key}"] = arr
+    num, pos = _coord(test / "test_singlepoint" / "mols" / "MB16_43_01" / "coord", symbols)
+    g["MB16_43_01/numbers"] = num
+    g["MB16_43_01/positions"] = pos
+    src["solv/*"] = (
+        "test/test_solvation/samples.py refs (tblite): psi, born, energies (ALPB p16, "
+        "eps 78.9), energies_still (GB Still), charges, gsolv and gradient (GFN1 + ALPB)"
+    )
+    src["MB16_43_01/*"] = "test/test_singlepoint/mols/MB16_43_01/coord"
     np.savez_compressed(HERE / "golden.npz", **g)
     (HERE / "golden_sources.json").write_text(json.dumps(src, indent=1))
 

@@ -117,3 +117,45 @@ def test_oracle_gradient_matches_finite_differences():
         ep = X.singlepoint("gfn2", num, pp, tol=1e-13).energy
         em = X.singlepoint("gfn2", num, pm, tol=1e-13).energy
         assert abs((ep - em) / (2 * h) - g[a, x]) < 1e-7
+
+
+# ---- generalized Born / ALPB solvation (test/test_solvation/samples.py, tblite) ----
+
+
+@pytest.mark.parametrize("name", ["MB16_43_01", "SiH4"])
+def test_born_radii_and_psi(name):
+    """OBC descreening integral and Born radii with the D3 vdW radii table."""
+    from dxtb_gb300.data import radii
+    from oracle import solvation_oracle as S
+
+    z = G[f"{name}/numbers"]
+    x = torch.tensor(G[f"{name}/positions"])
+    born, psi = S.born_radii(x, torch.tensor(radii.lookup(radii.VDW_D3, z, "vdw")))
+    assert np.abs(psi.numpy() / G[f"solv/{name}/psi"] - 1).max() < 1e-10
+    assert np.abs(born.numpy() / G[f"solv/{name}/born"] - 1).max() < 1e-10
+
+
+@pytest.mark.parametrize("kernel,alpb,key", [("p16", True, "energies"), ("still", False, "energies_still")])
+def test_gb_atom_energies(kernel, alpb, key):
+    """E_i = 1/2 q_i (A q)_i at fixed charges, eps = 78.9 (test_alpb.py:48-90)."""
+    from oracle import solvation_oracle as S
+
+    z = G["MB16_43_01/numbers"]
+    x = torch.tensor(G["MB16_43_01/positions"])
+    e = S.atom_energies(z, x, G["solv/MB16_43_01/charges"], epsilon=78.9, alpb=alpb, kernel=kernel)
+    # the reference's own tolerance is sqrt(eps) * 10 = 1.5e-7
+    assert np.abs(e.numpy() - G[f"solv/MB16_43_01/{key}"]).max() < 5e-9
+
+
+def test_gfn1_alpb_solvation_energy_and_gradient():
+    """GFN1 + ALPB (p16, eps 78.9) SCF: solvation energy and SCF-energy gradient
+    of MB16_43_01 (test_alpb.py::test_gb_scf, test_grad.py::test_gb_scf_grad)."""
+    z = G["MB16_43_01/numbers"]
+    x = G["MB16_43_01/positions"]
+    vac = X.singlepoint("gfn1", z, x, tol=1e-10, exclude=("rep",))
+    sol = X.singlepoint("gfn1", z, x, tol=1e-10, solvation={"epsilon": 78.9}, grad=True,
+                        exclude=("rep",))
+    gsolv = G["solv/MB16_43_01/gsolv"].sum()
+    assert abs((sol.e_elec - vac.e_elec) - gsolv) < 1e-7
+    # the fixture differentiates E_scf (no -TS); the reference's tolerance is 1e-5
+    assert np.abs(sol.extra["gradient"].numpy() - G["solv/MB16_43_01/gradient"]).max() < 1e-5
