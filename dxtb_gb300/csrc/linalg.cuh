@@ -177,7 +177,7 @@ __device__ void cta_tridiag(int n, double *A, double *d, double *e, double *tau,
       // column r (coalesced over r). The c range is split into G groups so
       // that all threads work; partials in smem, p^T v fused in.
       const double *A22 = A + (size_t)(k + 1) * n + (k + 1);
-      const int G = m < (int)blockDim.x ? min(256 / m, (int)blockDim.x / m) : 1;
+      const int G = m < (int)blockDim.x ? max(1, min(256 / m, (int)blockDim.x / m)) : 1;
       for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
         const int r = q % m, g = q / m;
         double s = 0.0;
@@ -569,7 +569,7 @@ __device__ void cta_back_transform(int n, const double *A, const double *tau, do
     double *Yb = Y + (size_t)(k + 1) * m;
     // w_j = t * v . Y[:, j]; the r range split into G groups (all threads busy)
     __shared__ double s_bpart[256];
-    const int G = m < (int)blockDim.x ? min(256 / m, (int)blockDim.x / m) : 1;
+    const int G = m < (int)blockDim.x ? max(1, min(256 / m, (int)blockDim.x / m)) : 1;
     for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
       const int j = q % m, g = q / m;
       double s = 0.0;

@@ -18,7 +18,7 @@ namespace dxtb {
 
 constexpr int kScfThreads = 256;     // CTA size for molecules sharing an SM
 constexpr int kScfBigThreads = 512;  // CTA size for large molecules on their own SM
-constexpr int kRank = 64;         // rank of the Broyden inverse-Jacobian memory
+constexpr int kRank = 256;        // Broyden inverse-Jacobian memory (the reference keeps all updates; >= maxiter)
 constexpr double kDamp = 0.5;     // step damping of the root solver (defaults.DAMP)
 constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
 constexpr double kOccCut = 1e-15; // orbitals below this occupation carry no density

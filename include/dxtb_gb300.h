@@ -280,8 +280,10 @@ int32_t dxtb_born_gradient(const dxtb_batch *b, const double *par_f,
  * process exits) instead of caller memory. A batch whose workspace
  * (sum over molecules of dxtb_scf_workspace_mol plus nmol + 2 header words)
  * does not fit returns DXTB_ERR_TOO_LARGE without running.
- * The first call on a device looks up the array's device address (set-up);
- * make that first call before any stream capture. All calls share the one
+ * The first call on a device looks up the array's device address, and the
+ * first call from each CUDA stream creates that stream's side stream and
+ * fork/join events for the large-molecule kernel (set-up, no device
+ * memory); make those first calls before any stream capture. All calls share the one
  * array, which keeps the last call's contents (nothing in it needs to start
  * at zero): calls that overlap on the GPU (other streams, other threads)
  * race and must be serialised by the caller. The call synchronises the
