@@ -1,24 +1,94 @@
-// CTA-level dense float64 linear algebra for one molecule's AO matrices
-// (row-major, leading dimension n, resident in global memory / L2). Every
-// routine must be called by all threads of the block.
+// Dense float64 linear algebra for one molecule's AO matrices (row-major,
+// leading dimension n, resident in global memory / L2), executed by a TEAM:
+// the CTAs of one thread-block cluster (or a single CTA). Every routine must
+// be called by all threads of all CTAs of the team, the same number of
+// times; each ends with a team barrier unless stated otherwise.
 //
 // The symmetric eigenproblem of the SCF is solved as
-//   Householder tridiagonalisation  (cta_tridiag)
-//   -> eigenvalues by implicit QL without vectors (cta_tql_values)
+//   Householder tridiagonalisation  (team_tridiag: the CTAs share the rows
+//     of the trailing matrix, two team barriers per reflector)
+//   -> eigenvalues: float32 bisection + float64 Newton, one thread each
+//      (team_tri_eigenvalues)
 //   -> eigenvectors of the lowest m eigenvalues only, by inverse iteration
 //      with a pivoted tridiagonal LU, one thread per eigenvalue cluster,
-//      Gram-Schmidt inside clusters (cta_tri_vectors)
-//   -> back-transformation of those m vectors (cta_back_transform).
+//      Gram-Schmidt inside clusters (team_tri_vectors)
+//   -> back-transformation of those m vectors, each CTA a block of
+//      vectors (team_back_transform: no team barrier per reflector).
 // The SCF needs only the orbitals with non-vanishing occupation, so the
 // O(n^3) accumulation of QL rotations is never done.
+//
+// In a cluster team, data written by another CTA is read with ld.global.cg
+// (L2, never a stale L1 line) after a barrier.cluster arrive.release /
+// wait.acquire pair; a one-CTA team uses plain loads and __syncthreads.
 #pragma once
 #include "common.cuh"
 
 namespace dxtb {
 
-// Shapes of the k-loop for triangular operands.
-constexpr int kTriSmem = 512;  // Householder vectors in shared memory up to this order
+constexpr int kPart = 512;  // shared partial sums of the split dot products
 
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// The CTAs that solve one molecule. CL: a thread-block cluster of `size`
+// CTAs; otherwise one CTA (size 1).
+template <bool CL>
+struct Team {
+  int rank, size;   // CTA rank in the team, number of CTAs
+  int tid, nthr;    // thread index over the team (rank-major), threads of the team
+  int stid;         // thread index with consecutive values on different CTAs
+  double *gred;     // global scratch [32]: CTA partial sums, two alternating slots
+  int *gctl;        // global scratch [16]: words broadcast by rank 0
+  int phase;
+  __device__ __forceinline__ void sync() {
+    if constexpr (CL) cluster_barrier(); else __syncthreads();
+  }
+  __device__ __forceinline__ bool lead() const { return rank == 0; }
+};
+
+// Load of data that another CTA of the team may have written.
+template <bool CL>
+__device__ __forceinline__ double ld(const double *p) {
+  if constexpr (CL) return __ldcg(p); else return *p;
+}
+template <bool CL>
+__device__ __forceinline__ int ldi(const int *p) {
+  if constexpr (CL) return __ldcg(p); else return *p;
+}
+
+// Sum over the team (every thread gets it); CTA partials combined in rank order.
+template <bool CL>
+__device__ double team_sum(Team<CL> &tm, double v, double *red) {
+  double s = block_sum(v, red);
+  if constexpr (CL) {
+    if (tm.size > 1) {
+      double *slot = tm.gred + 16 * (tm.phase & 1);
+      ++tm.phase;
+      if (threadIdx.x == 0) slot[tm.rank] = s;
+      tm.sync();
+      s = 0.0;
+      for (int c = 0; c < tm.size; ++c) s += __ldcg(slot + c);
+    }
+  }
+  return s;
+}
+
+// Shapes of the k-loop for triangular operands.
 enum KRange : int {
   kFull = 0,     // k in [0, K)
   kALower = 1,   // op(A)(i,k) = 0 for k > i   -> k < i0 + 4
@@ -28,17 +98,46 @@ enum KRange : int {
 
 // C = alpha * op(A) op(B) + beta * C for M x N outputs and inner size K.
 // op(A)(i,k) = TA ? A[k*lda+i] : A[i*lda+k]; op(B)(k,j) = TB ? B[j*ldb+k] : B[k*ldb+j].
-// Register tile of 4 x 4 outputs per thread. With lower_only, tiles strictly
-// above the diagonal are skipped (symmetric results). The FP64 pipe, not
-// memory, is the limit at these sizes.
-template <bool TA, bool TB>
-__device__ void cta_gemm(int M, int N, int K, double alpha, const double *__restrict__ A, int lda,
-                         const double *__restrict__ B, int ldb, double beta, double *__restrict__ C,
-                         int ldc, int krange = kFull, bool lower_only = false) {
-  const int tm = (M + 3) >> 2, tn = (N + 3) >> 2;
-  for (int t = threadIdx.x; t < tm * tn; t += blockDim.x) {
-    const int i0 = (t / tn) * 4, j0 = (t % tn) * 4;
-    if (lower_only && j0 > i0 + 3) continue;
+// Register tile of 4 x 4 outputs per thread, tiles spread over the team.
+// With lower_only, tiles strictly above the diagonal are skipped
+// (symmetric results). The FP64 pipe, not memory, is the limit.
+template <bool TA, bool TB, bool CL>
+__device__ void team_gemm(Team<CL> &tm, int M, int N, int K, double alpha, const double *A, int lda,
+                          const double *B, int ldb, double beta, double *C, int ldc,
+                          int krange = kFull, bool lower_only = false) {
+  const int tmm = (M + 3) >> 2, tnn = (N + 3) >> 2;
+  // Tiles are enumerated so that one round of the team's threads gets tiles
+  // of similar k-length (the k-range follows the tile row for kALower and
+  // the tile column otherwise); lower_only enumerates the tiles on and below
+  // the diagonal only (M == N).
+  const bool col_slow = (krange == kBLowerT || krange == kBUpper);
+  const int ntile = lower_only ? tmm * (tmm + 1) / 2 : tmm * tnn;
+  for (int t = tm.tid; t < ntile; t += tm.nthr) {
+    int ti, tj;
+    if (lower_only) {
+      if (col_slow) {
+        // column-major over the lower triangle: column tj holds tmm - tj tiles
+        const int u = ntile - 1 - t;  // reverse: count from the short last columns
+        int c = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+        while ((c + 1) * (c + 2) / 2 <= u) ++c;
+        while (c * (c + 1) / 2 > u) --c;
+        tj = tmm - 1 - c;
+        ti = tmm - 1 - (u - c * (c + 1) / 2);
+      } else {
+        int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((r + 1) * (r + 2) / 2 <= t) ++r;
+        while (r * (r + 1) / 2 > t) --r;
+        ti = r;
+        tj = t - r * (r + 1) / 2;
+      }
+    } else if (col_slow) {
+      tj = t / tmm;
+      ti = t % tmm;
+    } else {
+      ti = t / tnn;
+      tj = t % tnn;
+    }
+    const int i0 = ti * 4, j0 = tj * 4;
     double acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -57,9 +156,11 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *__rest
     for (int k = k0; k < k1; ++k) {
       double av[4], bv[4];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) av[a] = TA ? A[(size_t)k * lda + ia[a]] : A[(size_t)ia[a] * lda + k];
+      for (int a = 0; a < 4; ++a)
+        av[a] = ld<CL>(TA ? A + (size_t)k * lda + ia[a] : A + (size_t)ia[a] * lda + k);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) bv[c] = TB ? B[(size_t)jb[c] * ldb + k] : B[(size_t)k * ldb + jb[c]];
+      for (int c = 0; c < 4; ++c)
+        bv[c] = ld<CL>(TB ? B + (size_t)jb[c] * ldb + k : B + (size_t)k * ldb + jb[c]);
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -72,225 +173,158 @@ __device__ void cta_gemm(int M, int N, int K, double alpha, const double *__rest
         const int i = i0 + a, j = j0 + c;
         if (i < M && j < N && (!lower_only || j <= i)) {
           double *p = C + (size_t)i * ldc + j;
-          *p = alpha * acc[a][c] + (beta == 0.0 ? 0.0 : beta * *p);
+          *p = alpha * acc[a][c] + (beta == 0.0 ? 0.0 : beta * ld<CL>(p));
         }
       }
   }
-  __syncthreads();
+  tm.sync();
 }
 
 // Copy the lower triangle of a square matrix onto its upper triangle.
-__device__ void cta_mirror_lower(int n, double *A) {
-  for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+template <bool CL>
+__device__ void team_mirror_lower(Team<CL> &tm, int n, double *A) {
+  for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
     const int i = (int)(t / n), j = (int)(t % n);
-    if (j > i) A[t] = A[(size_t)j * n + i];
+    if (j > i) A[t] = ld<CL>(A + (size_t)j * n + i);
   }
-  __syncthreads();
+  tm.sync();
 }
 
 // In-place lower Cholesky factor of a symmetric positive-definite matrix
-// (right-looking). Returns false if a pivot is not positive.
-__device__ bool cta_cholesky(int n, double *A) {
-  __shared__ int s_bad;
-  if (threadIdx.x == 0) s_bad = 0;
-  __syncthreads();
+// (right-looking, the trailing update spread over the team). Returns false
+// (on every thread) if a pivot is not positive.
+template <bool CL>
+__device__ bool team_cholesky(Team<CL> &tm, int n, double *A) {
   for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      const double dkk = A[(size_t)k * n + k];
-      if (!(dkk > 0.0)) s_bad = 1;
-      A[(size_t)k * n + k] = sqrt(fmax(dkk, kTiny));
-    }
-    __syncthreads();
-    if (s_bad) return false;
-    const double lkk = A[(size_t)k * n + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(size_t)i * n + k] /= lkk;
-    __syncthreads();
+    const double dkk = ld<CL>(A + (size_t)k * n + k);
+    if (!(dkk > 0.0)) return false;  // every thread read the same value
+    const double lkk = sqrt(dkk);
+    for (int i = k + 1 + tm.tid; i < n; i += tm.nthr) A[(size_t)i * n + k] = ld<CL>(A + (size_t)i * n + k) / lkk;
+    tm.sync();
+    if (tm.lead() && threadIdx.x == 0) A[(size_t)k * n + k] = lkk;
     const int m = n - k - 1;
-    for (int64_t t = threadIdx.x; t < (int64_t)m * m; t += blockDim.x) {
+    for (int64_t t = tm.tid; t < (int64_t)m * m; t += tm.nthr) {
       const int i = k + 1 + (int)(t / m), j = k + 1 + (int)(t % m);
-      if (j <= i) A[(size_t)i * n + j] -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+      if (j <= i)
+        A[(size_t)i * n + j] = ld<CL>(A + (size_t)i * n + j) -
+                               ld<CL>(A + (size_t)i * n + k) * ld<CL>(A + (size_t)j * n + k);
     }
-    __syncthreads();
+    tm.sync();
   }
   return true;
 }
 
 // X = L^-1 for a lower-triangular L (row-major); upper part of X zeroed.
-// Thread j solves column j by forward substitution.
-__device__ void cta_trinv(int n, const double *L, double *X) {
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+// Thread j of the team solves column j by forward substitution.
+template <bool CL>
+__device__ void team_trinv(Team<CL> &tm, int n, const double *L, double *X) {
+  for (int j = tm.stid; j < n; j += tm.nthr) {
     for (int i = 0; i < j; ++i) X[(size_t)i * n + j] = 0.0;
-    X[(size_t)j * n + j] = 1.0 / L[(size_t)j * n + j];
+    X[(size_t)j * n + j] = 1.0 / ld<CL>(L + (size_t)j * n + j);
     for (int i = j + 1; i < n; ++i) {
       double s = 0.0;
-      for (int k = j; k < i; ++k) s = fma(L[(size_t)i * n + k], X[(size_t)k * n + j], s);
-      X[(size_t)i * n + j] = -s / L[(size_t)i * n + i];
+      for (int k = j; k < i; ++k) s = fma(ld<CL>(L + (size_t)i * n + k), X[(size_t)k * n + j], s);
+      X[(size_t)i * n + j] = -s / ld<CL>(L + (size_t)i * n + i);
     }
   }
-  __syncthreads();
+  tm.sync();
 }
 
 // Householder reduction of a full symmetric matrix to tridiagonal form
 // (lower variant): A = Q T Q^T. On exit d, e hold the diagonal and
 // sub-diagonal (e[i] couples i and i+1), the reflector of step k is stored
-// in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k].
-__device__ void cta_tridiag(int n, double *A, double *d, double *e, double *tau, double *p,
-                            double *vbuf, double *red) {
-  // The Householder vector and p live in shared memory when they fit.
-  __shared__ double s_v[kTriSmem], s_p[kTriSmem];
-  __shared__ double s_part[256];
-  double *sv = n <= kTriSmem ? s_v : vbuf;
-  double *sp = n <= kTriSmem ? s_p : p;
+// in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k]; d, e, tau
+// are written by the lead CTA. At step k every CTA holds the Householder
+// vector v and p = t A22 v - K v in shared memory (sv, sp: n doubles each),
+// and owns one contiguous chunk of the trailing rows: it forms those entries
+// of A22 v and applies the rank-2 update to those rows. pg: global [n]
+// exchange buffer for p. spart: shared [kPart].
+template <bool CL>
+__device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *e, double *tau,
+                             double *pg, double *sv, double *sp, double *spart, double *red) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
-    double *col = A + (size_t)(k + 1) * n + k;  // col[r*n], r < m
+    const double *col = A + (size_t)(k + 1) * n + k;  // col[r*n], r < m
     double part = 0.0;
     for (int r = threadIdx.x; r < m; r += blockDim.x) {
-      const double x = col[(size_t)r * n];
+      const double x = ld<CL>(col + (size_t)r * n);
       sv[r] = x;
       if (r > 0) part += x * x;
     }
     const double sigma = block_sum(part, red);  // also orders the sv writes
-    const double alpha = col[0];  // not sv[0]: thread 0 overwrites it below
+    const double alpha = ld<CL>(col);
     double t = 0.0, beta = alpha;
     if (sigma > 0.0) {
       const double nrm = sqrt(alpha * alpha + sigma);
       beta = alpha >= 0.0 ? -nrm : nrm;
       t = (beta - alpha) / beta;
       const double scale = 1.0 / (alpha - beta);
-      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) {
-        const double v = sv[r] * scale;
-        sv[r] = v;
-        col[(size_t)r * n] = v;  // kept for the back-transformation
-      }
+      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) sv[r] *= scale;
     }
-    if (threadIdx.x == 0) {
-      sv[0] = 1.0;
+    if (threadIdx.x == 0) sv[0] = 1.0;
+    if (tm.lead() && threadIdx.x == 0) {
       tau[k] = t;
       e[k] = beta;
-      d[k] = A[(size_t)k * n + k];
+      d[k] = ld<CL>(A + (size_t)k * n + k);
     }
     __syncthreads();
-    if (t != 0.0) {
-      // p = t * A22 v; A22 is symmetric, so row r of the product reads
-      // column r (coalesced over r). The c range is split into G groups so
-      // that all threads work; partials in smem, p^T v fused in.
-      const double *A22 = A + (size_t)(k + 1) * n + (k + 1);
-      const int G = m < (int)blockDim.x ? max(1, min(256 / m, (int)blockDim.x / m)) : 1;
-      for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
-        const int r = q % m, g = q / m;
+    if (t != 0.0) {  // the same on every CTA of the team
+      const int r0 = (int)((int64_t)m * tm.rank / tm.size);
+      const int r1 = (int)((int64_t)m * (tm.rank + 1) / tm.size);
+      const int mc = r1 - r0;
+      double *A22 = A + (size_t)(k + 1) * n + (k + 1);
+      double *pdst = CL ? pg : sp;
+      // p_r = t (A22 v)_r for the own rows; A22 is symmetric, so row r of the
+      // product reads column r (coalesced over r); the c range is split in G
+      // groups so that all threads work
+      const int G = (mc > 0 && mc < (int)blockDim.x) ? max(1, min(kPart / mc, (int)blockDim.x / mc)) : 1;
+      for (int q = threadIdx.x; q < G * mc; q += blockDim.x) {
+        const int rr = q % mc, g = q / mc, r = r0 + rr;
         double s = 0.0;
-        for (int c = g; c < m; c += G) s = fma(A22[(size_t)c * n + r], sv[c], s);
-        if (G > 1) s_part[g * m + r] = s; else sp[r] = t * s;
+        for (int c = g; c < m; c += G) s = fma(ld<CL>(A22 + (size_t)c * n + r), sv[c], s);
+        if (G > 1) spart[g * mc + rr] = s; else pdst[r] = t * s;
       }
-      __syncthreads();
+      if (G > 1) {
+        __syncthreads();
+        for (int rr = threadIdx.x; rr < mc; rr += blockDim.x) {
+          double s = 0.0;
+          for (int g = 0; g < G; ++g) s += spart[g * mc + rr];
+          pdst[r0 + rr] = t * s;
+        }
+      }
+      tm.sync();  // p complete over the team
       double part2 = 0.0;
       for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        double pr;
-        if (G > 1) {
-          double s = 0.0;
-          for (int g = 0; g < G; ++g) s += s_part[g * m + r];
-          pr = t * s;
-          sp[r] = pr;
-        } else {
-          pr = sp[r];
-        }
+        const double pr = CL ? __ldcg(pg + r) : sp[r];
+        if (CL) sp[r] = pr;
         part2 += pr * sv[r];
       }
       const double K = 0.5 * t * block_sum(part2, red);
       for (int r = threadIdx.x; r < m; r += blockDim.x) sp[r] -= K * sv[r];
+      // keep v (own rows) in column k for the back-transformation
+      for (int r = max(r0, 1) + threadIdx.x; r < r1; r += blockDim.x) A[(size_t)(k + 1 + r) * n + k] = sv[r];
       __syncthreads();
-      // rank-2 update, rows over warps, columns over lanes (coalesced)
-      double *W = A + (size_t)(k + 1) * n + (k + 1);
-      for (int r = ty; r < m; r += nty) {
+      // rank-2 update of the own rows, columns over lanes (coalesced)
+      for (int r = r0 + ty; r < r1; r += nty) {
         const double vr = sv[r], pr = sp[r];
-        double *Wr = W + (size_t)r * n;
-        for (int c = tx; c < m; c += 32) Wr[c] -= vr * sp[c] + pr * sv[c];
+        double *Wr = A22 + (size_t)r * n;
+        for (int c = tx; c < m; c += 32) Wr[c] = fma(-vr, sp[c], fma(-pr, sv[c], ld<CL>(Wr + c)));
       }
     }
-    __syncthreads();
+    tm.sync();  // the next column is complete
   }
-  if (threadIdx.x == 0) {
+  if (tm.lead() && threadIdx.x == 0) {
     if (n >= 2) {
-      d[n - 2] = A[(size_t)(n - 2) * n + (n - 2)];
-      e[n - 2] = A[(size_t)(n - 1) * n + (n - 2)];
+      d[n - 2] = ld<CL>(A + (size_t)(n - 2) * n + (n - 2));
+      e[n - 2] = ld<CL>(A + (size_t)(n - 1) * n + (n - 2));
       tau[n - 2] = 0.0;
     }
-    d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)];
+    d[n - 1] = ld<CL>(A + (size_t)(n - 1) * n + (n - 1));
     e[n - 1] = 0.0;
     tau[n - 1] = 0.0;
   }
-  __syncthreads();
-}
-
-// Eigenvalues of the symmetric tridiagonal (d, e) by implicit QL with
-// Wilkinson-type shifts (Bowdler, Martin, Reinsch, Wilkinson, Numer. Math.
-// 11, 293 (1968)), without eigenvector accumulation. Thread 0 runs the
-// scalar recurrence on the scratch copies sd, se (shared memory when they
-// fit); lam receives the (unsorted) eigenvalues. False if an eigenvalue
-// needs more than 60 sweeps.
-__device__ bool cta_tql_values(int n, const double *d, const double *e, double *sd, double *se,
-                               double *lam) {
-  __shared__ int s_ok;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    sd[i] = d[i];
-    se[i] = e[i];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    for (int l = 0; l < n && ok; ++l) {
-      int iter = 0;
-      while (true) {
-        int m = l;
-        for (; m < n - 1; ++m) {
-          const double dd = fabs(sd[m]) + fabs(sd[m + 1]);
-          if (fabs(se[m]) <= kEps * dd) break;
-        }
-        if (m == l) break;
-        if (++iter > 60) {
-          ok = 0;
-          break;
-        }
-        double g = (sd[l + 1] - sd[l]) / (2.0 * se[l]);
-        double r = sqrt(g * g + 1.0);
-        g = sd[m] - sd[l] + se[l] / (g + copysign(r, g));
-        double s = 1.0, c = 1.0, p = 0.0;
-        int i = m - 1;
-        bool early = false;
-        for (; i >= l; --i) {
-          const double f = s * se[i], bb = c * se[i];
-          r = sqrt(f * f + g * g);
-          se[i + 1] = r;
-          if (r == 0.0) {
-            sd[i + 1] -= p;
-            se[m] = 0.0;
-            early = true;
-            break;
-          }
-          const double ir = 1.0 / r;
-          s = f * ir;
-          c = g * ir;
-          g = sd[i + 1] - p;
-          r = (sd[i] - g) * s + 2.0 * c * bb;
-          p = s * r;
-          sd[i + 1] = g + p;
-          g = c * r - bb;
-        }
-        if (!early) {
-          sd[l] -= p;
-          se[l] = g;
-          se[m] = 0.0;
-        }
-      }
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sd[i];
-  __syncthreads();
-  return s_ok != 0;
+  tm.sync();
 }
 
 // Number of eigenvalues of the tridiagonal (d, e) below x (Sturm count of
@@ -302,68 +336,97 @@ __device__ __forceinline__ int sturm_count_f32(int n, const float *d, const floa
   if (q == 0.0f) q = -tiny;
   cnt += q < 0.0f;
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - e2[i - 1] / q;
+    q = (d[i] - x) - __fdividef(e2[i - 1], q);
     if (q == 0.0f) q = -tiny;
     cnt += q < 0.0f;
   }
   return cnt;
 }
 
-// The same count in float64 (robust fallback).
-__device__ __forceinline__ int sturm_count_f64(int n, const double *d, const double *e, double x,
-                                               double tiny) {
-  int cnt = 0;
-  double q = d[0] - x;
-  if (q == 0.0) q = -tiny;
-  cnt += q < 0.0;
+__device__ __forceinline__ bool is_neg(double v) { return __double_as_longlong(v) < 0; }
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+// |v| outside [2^-500, 2^500] (biased exponent test, no FP64 instruction)
+__device__ __forceinline__ bool out_of_range(double v) {
+  const int ex = (int)((__double_as_longlong(v) >> 52) & 0x7ff);
+  return ex > 1023 + 500 || (ex < 1023 - 500 && ex != 0);
+}
+
+// The same count in float64 without divisions: the pivots of T - x I are
+// q_k = p_k / p_{k-1} for the leading principal minors p_k = det(T_k - x I)
+// (three-term recurrence, e2 = e^2), so a negative pivot is a sign change
+// between p_{k-1} and p_k. A zero minor counts as a change, like a zero
+// pivot replaced by -tiny, and continues as a tiny value of that sign; the
+// pair (p_{k-1}, p_k) is rescaled (every 8 steps) to stay in range.
+__device__ __forceinline__ int sturm_count_f64(int n, const double *d, const double *e2, double x) {
+  double p0 = 1.0, p1 = d[0] - x;
+  bool neg1 = is_neg(p1) || is_zero(p1);
+  if (is_zero(p1)) p1 = -1e-300;
+  int cnt = neg1 ? 1 : 0;
   for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
-    if (q == 0.0) q = -tiny;
-    cnt += q < 0.0;
+    double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+    bool neg2 = is_neg(p2);
+    if (is_zero(p2)) {
+      neg2 = !neg1;
+      p2 = neg2 ? -1e-300 : 1e-300;
+    }
+    cnt += neg2 != neg1;
+    neg1 = neg2;
+    p0 = p1;
+    p1 = p2;
+    if ((i & 7) == 0 && (out_of_range(p0) || out_of_range(p1))) {
+      const double sc = (fabs(p1) + fabs(p0)) > 1.0 ? 0x1p-500 : 0x1p500;
+      p0 *= sc;
+      p1 *= sc;
+    }
   }
   return cnt;
 }
 
-// Characteristic polynomial p(x) = det(T - x I) of the leading principal
-// minors and its derivative, by the three-term recurrence with rescaling
-// (no divisions); returns p / p' (the Newton correction is -p/p').
-__device__ __forceinline__ double charpoly_ratio(int n, const double *d, const double *e, double x) {
+// Characteristic polynomial p(x) = det(T - x I) and its derivative by the
+// three-term recurrence (e2 = e^2), rescaled every 8 steps; returns p / p'.
+__device__ __forceinline__ double charpoly_ratio(int n, const double *d, const double *e2, double x) {
   double p0 = 1.0, p1 = d[0] - x;   // p_{k-1}, p_k
   double q0 = 0.0, q1 = -1.0;       // p'_{k-1}, p'_k
   for (int i = 1; i < n; ++i) {
-    const double di = d[i] - x, e2 = e[i - 1] * e[i - 1];
-    const double p2 = di * p1 - e2 * p0;
-    const double q2 = -p1 + di * q1 - e2 * q0;
+    const double di = d[i] - x, ee = e2[i - 1];
+    const double p2 = fma(di, p1, -ee * p0);
+    const double q2 = fma(di, q1, -fma(ee, q0, p1));
     p0 = p1;
     p1 = p2;
     q0 = q1;
     q1 = q2;
-    const double big = fmax(fabs(p1), fabs(q1));
-    if (big > 1e150) {
-      p0 *= 1e-150; p1 *= 1e-150; q0 *= 1e-150; q1 *= 1e-150;
-    } else if (big < 1e-150 && big > 0.0) {
-      p0 *= 1e150; p1 *= 1e150; q0 *= 1e150; q1 *= 1e150;
+    if ((i & 7) == 0 && (out_of_range(p1) || out_of_range(q1) || out_of_range(p0) || out_of_range(q0))) {
+      const double big = fmax(fmax(fabs(p1), fabs(q1)), fmax(fabs(p0), fabs(q0)));
+      const double sc = big > 1.0 ? 0x1p-500 : 0x1p500;
+      p0 *= sc; p1 *= sc; q0 *= sc; q1 *= sc;
     }
   }
   return q1 != 0.0 ? p1 / q1 : 0.0;
 }
 
-// All eigenvalues of the symmetric tridiagonal (d, e), ascending, one per
-// thread: float32 bisection on Sturm counts isolates eigenvalue k to ~1e-7
-// relative, float64 Newton steps on the characteristic polynomial refine it,
-// and a float64 Sturm count checks that the result is the k-th eigenvalue;
-// eigenvalues that fail (clusters closer than the float32 resolution) are
-// recomputed by float64 bisection. df/e2f: float scratch of n each.
-__device__ void cta_tri_eigenvalues(int n, const double *d, const double *e, double *lam,
-                                    float *df, float *e2f) {
+// All eigenvalues of the symmetric tridiagonal (d, e) (shared-memory copies
+// held by every CTA), one per thread of the team. Float32 bisection on Sturm
+// counts isolates eigenvalue k to ~1e-7 relative. Float64 Sturm counts then
+// confirm that the bracket holds only the k-th eigenvalue, bisecting a few
+// more times where a near-degenerate neighbour shares it. Safeguarded
+// float64 Newton steps on the characteristic polynomial refine the isolated
+// root. Eigenvalues closer than the float64 resolution of the counts keep
+// the bracket midpoint (their vectors come from one cluster). df/e2f: shared
+// float scratch of n each, e2: shared double scratch of n. lam: global,
+// ascending index k.
+template <bool CL>
+__device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const double *e,
+                                     double *e2, double *lam, float *df, float *e2f) {
   __shared__ double s_gl, s_gu;
   double gl = 1e308, gu = -1e308;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
     gl = fmin(gl, d[i] - r);
     gu = fmax(gu, d[i] + r);
+    const double ee = i < n - 1 ? e[i] * e[i] : 0.0;
+    e2[i] = ee;
     df[i] = (float)d[i];
-    e2f[i] = i < n - 1 ? (float)(e[i] * e[i]) : 0.0f;
+    e2f[i] = (float)ee;
   }
   gl = -warp_max(-gl);
   gu = warp_max(gu);
@@ -385,8 +448,7 @@ __device__ void cta_tri_eigenvalues(int n, const double *d, const double *e, dou
   const double span = s_gu - s_gl;
   const double glo = s_gl - 1e-6 * span - 1e-12, ghi = s_gu + 1e-6 * span + 1e-12;
   const float tinyf = 1e-30f;
-  const double tiny = 1e-300;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+  for (int k = tm.stid; k < n; k += tm.nthr) {
     // --- float32 bisection: count(lo) <= k < count(hi) ---
     float lo = (float)glo, hi = (float)ghi;
     for (int it = 0; it < 60; ++it) {
@@ -395,55 +457,73 @@ __device__ void cta_tri_eigenvalues(int n, const double *d, const double *e, dou
       if (sturm_count_f32(n, df, e2f, mid, tinyf) <= k) lo = mid; else hi = mid;
     }
     const double w32 = fmax((double)hi - (double)lo, 4e-7 * tnorm + 1e-12);
-    double x = 0.5 * ((double)lo + (double)hi);
-    const double blo = x - 4.0 * w32, bhi = x + 4.0 * w32;
-    // --- float64 Newton on p(x) ---
-    bool ok = true;
-    for (int it = 0; it < 4; ++it) {
-      const double dx = charpoly_ratio(n, d, e, x);
-      x -= dx;
-      if (!(x > blo && x < bhi)) { ok = false; break; }
-      if (fabs(dx) <= 2.0 * kEps * fmax(fabs(x), 1e-3 * tnorm)) break;
+    const double x0 = 0.5 * ((double)lo + (double)hi);
+    // --- float64 bracket [l, h) with count(l) <= k < count(h) ---
+    double l = x0 - 4.0 * w32, h = x0 + 4.0 * w32;
+    int cl = sturm_count_f64(n, d, e2, l), ch = sturm_count_f64(n, d, e2, h);
+    if (!(cl <= k && k < ch)) {
+      l = glo;
+      h = ghi;
+      cl = 0;
+      ch = n;
     }
-    // --- check the index with float64 Sturm counts (eigenvalues closer than
-    // del are interchangeable: their vectors come from one cluster) ---
-    const double del = 1e-12 * fmax(tnorm, 1.0);
-    if (ok) {
-      const int cl = sturm_count_f64(n, d, e, x - del, tiny);
-      const int ch = sturm_count_f64(n, d, e, x + del, tiny);
-      ok = (cl <= k && k < ch);
+    // --- bisect until the bracket holds the k-th eigenvalue alone ---
+    for (int it = 0; it < 200 && !(cl == k && ch == k + 1); ++it) {
+      const double mid = 0.5 * (l + h);
+      if (mid <= l || mid >= h) break;
+      const int c = sturm_count_f64(n, d, e2, mid);
+      if (c <= k) {
+        l = mid;
+        cl = c;
+      } else {
+        h = mid;
+        ch = c;
+      }
     }
-    if (!ok) {
-      // --- float64 bisection inside the float32 bracket (widened) ---
-      double l = glo, h = ghi;
-      if (sturm_count_f64(n, d, e, blo, tiny) <= k && sturm_count_f64(n, d, e, bhi, tiny) > k) {
-        l = blo;
-        h = bhi;
+    double x = 0.5 * (l + h);
+    if (cl == k && ch == k + 1) {
+      // --- safeguarded Newton on p(x): one root in (l, h) ---
+      x = fmin(fmax(x0, l), h);
+      if (!(x > l && x < h)) x = 0.5 * (l + h);
+      // converged when the Newton step is at the rounding level of the
+      // recurrence (eps |T|); a step that would leave the bracket becomes a
+      // bisection step, and then (or after slow steps) the count at the new
+      // point shrinks the bracket
+      const double tol = 4.0 * kEps * fmax(tnorm, fabs(x));
+      for (int it = 0; it < 16; ++it) {
+        double xn = x - charpoly_ratio(n, d, e2, x);
+        const bool bis = !(xn > l && xn < h);
+        if (bis) xn = 0.5 * (l + h);
+        const double step = fabs(xn - x);
+        x = xn;
+        if (!bis && step <= tol) break;
+        if (bis || it >= 3) {
+          if (sturm_count_f64(n, d, e2, x) <= k) l = x; else h = x;
+          if (h - l <= tol) break;
+        }
       }
-      for (int it = 0; it < 200; ++it) {
-        const double mid = 0.5 * (l + h);
-        if (mid <= l || mid >= h) break;
-        if (sturm_count_f64(n, d, e, mid, tiny) <= k) l = mid; else h = mid;
-      }
-      x = 0.5 * (l + h);
     }
     lam[k] = x;
   }
-  __syncthreads();
+  tm.sync();
 }
 
-// Ascending sort by rank (ties broken by index): out[rank(i)] = in[i].
-__device__ void cta_rank_sort(int n, const double *in, double *out) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double v = in[i];
+// Ascending sort by rank (ties broken by index): out[rank(i)] = in[i]; in
+// is copied to the shared scratch s (n doubles) first. out: global.
+template <bool CL>
+__device__ void team_rank_sort(Team<CL> &tm, int n, const double *in, double *out, double *s) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = ld<CL>(in + i);
+  __syncthreads();
+  for (int i = tm.stid; i < n; i += tm.nthr) {
+    const double v = s[i];
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      const double u = in[j];
+      const double u = s[j];
       r += (u < v) || (u == v && j < i);
     }
     out[r] = v;
   }
-  __syncthreads();
+  tm.sync();
 }
 
 __device__ __forceinline__ double start_vector(int i, int j) {
@@ -461,28 +541,35 @@ __device__ __forceinline__ double start_vector(int i, int j) {
 // pivoted LU of T - lam I (the scheme of LAPACK's dstein: three solves,
 // re-orthogonalisation against the previous members of the cluster).
 // Clusters are runs of eigenvalues closer than ctol; each cluster is one
-// thread's work. Y: n x m row-major (column j = vector j).
-// lu: scratch of 5 * n * blockDim doubles. cl: int scratch of m + 1.
-__device__ void cta_tri_vectors(int n, const double *d, const double *e, const double *lam, int m,
-                                double tnorm, double *Y, double *lu, int *cl, int *s_ncl) {
+// thread's work (over the team). d, e, lam: shared copies. Y: n x m
+// row-major global (column j = vector j). lu: global scratch of
+// 5 * n * nslot doubles; team threads [0, nslot) factorise (nslot <= team
+// threads). cl: global int [m + 1]; the lead CTA lists the clusters, the
+// count goes through gctl[2].
+template <bool CL>
+__device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const double *e,
+                                 const double *lam, int m, double tnorm, double *Y, double *lu,
+                                 int nslot, int *cl) {
   const double ctol = 1e-6 * fmax(tnorm, 1.0);
   const double tiny = kEps * fmax(tnorm, 1.0);
-  if (threadIdx.x == 0) {
+  if (tm.lead() && threadIdx.x == 0) {
     int c = 0;
     cl[c++] = 0;
     for (int j = 1; j < m; ++j)
       if (lam[j] - lam[j - 1] > ctol) cl[c++] = j;
     cl[c] = m;
-    *s_ncl = c;
+    tm.gctl[2] = c;
   }
-  __syncthreads();
-  const int ncl = *s_ncl;
-  const int nthr = blockDim.x, tid = threadIdx.x;
-  double *U0 = lu, *U1 = lu + (size_t)n * nthr, *U2 = lu + 2 * (size_t)n * nthr;
-  double *Lm = lu + 3 * (size_t)n * nthr, *Pv = lu + 4 * (size_t)n * nthr;
-#define LU(arr, i) arr[(size_t)(i) * nthr + tid]
-  for (int c = tid; c < ncl; c += nthr) {
-    const int j0 = cl[c], j1 = cl[c + 1];
+  tm.sync();
+  const int ncl = ldi<CL>(tm.gctl + 2);
+  // factorisation slots: the first nslot threads in the spread order, so
+  // that the clusters are shared by the CTAs
+  const int tid = tm.stid;
+  double *U0 = lu, *U1 = lu + (size_t)n * nslot, *U2 = lu + 2 * (size_t)n * nslot;
+  double *Lm = lu + 3 * (size_t)n * nslot, *Pv = lu + 4 * (size_t)n * nslot;
+#define LU(arr, i) arr[(size_t)(i) * nslot + tid]
+  for (int c = tid; tid < nslot && c < ncl; c += nslot) {
+    const int j0 = ldi<CL>(cl + c), j1 = ldi<CL>(cl + c + 1);
     for (int j = j0; j < j1; ++j) {
       // separate exactly coincident shifts inside a cluster (dstein)
       const double lmb = lam[j] + (j - j0) * 10.0 * tiny;
@@ -521,17 +608,20 @@ __device__ void cta_tri_vectors(int n, const double *d, const double *e, const d
       for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
       const int nsolve = (j1 - j0 > 1) ? 3 : 2;
       for (int it = 0; it < nsolve; ++it) {
-        // forward: apply the row interchanges and multipliers
+        // forward: apply the row interchanges and multipliers (the running
+        // row stays in a register; the loads do not depend on the chain)
+        double carry = Y[j];
         for (int i = 0; i < n - 1; ++i) {
-          double xi = Y[(size_t)i * m + j], xn = Y[(size_t)(i + 1) * m + j];
+          double xi = carry, xn = Y[(size_t)(i + 1) * m + j];
           if (LU(Pv, i) != 0.0) {
             const double t = xi;
             xi = xn;
             xn = t;
           }
           Y[(size_t)i * m + j] = xi;
-          Y[(size_t)(i + 1) * m + j] = xn - LU(Lm, i) * xi;
+          carry = xn - LU(Lm, i) * xi;
         }
+        Y[(size_t)(n - 1) * m + j] = carry;
         // back substitution with the upper factor (two super-diagonals)
         double x1 = 0.0, x2 = 0.0;
         for (int i = n - 1; i >= 0; --i) {
@@ -554,44 +644,51 @@ __device__ void cta_tri_vectors(int n, const double *d, const double *e, const d
     }
   }
 #undef LU
-  __syncthreads();
+  tm.sync();
 }
 
-// Y <- Q Y for the reflectors stored by cta_tridiag (Q = H_0 ... H_{n-3});
-// Y is n x m row-major. w: scratch of m doubles.
-__device__ void cta_back_transform(int n, const double *A, const double *tau, double *Y, int m,
-                                   double *w) {
-  for (int k = n - 3; k >= 0; --k) {
-    const double t = tau[k];
-    if (t == 0.0) continue;
-    const int mm = n - k - 1;
-    const double *col = A + (size_t)(k + 1) * n + k;
-    double *Yb = Y + (size_t)(k + 1) * m;
-    // w_j = t * v . Y[:, j]; the r range split into G groups (all threads busy)
-    __shared__ double s_bpart[256];
-    const int G = m < (int)blockDim.x ? max(1, min(256 / m, (int)blockDim.x / m)) : 1;
-    for (int q = threadIdx.x; q < G * m; q += blockDim.x) {
-      const int j = q % m, g = q / m;
-      double s = 0.0;
-      for (int r = g; r < mm; r += G) s = fma(r == 0 ? 1.0 : col[(size_t)r * n], Yb[(size_t)r * m + j], s);
-      if (G > 1) s_bpart[g * m + j] = s; else w[j] = t * s;
-    }
-    __syncthreads();
-    if (G > 1) {
-      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+// Y <- Q Y for the reflectors stored by team_tridiag (Q = H_0 ... H_{n-3});
+// Y is n x m row-major. Each CTA transforms its own block of columns, so no
+// team barrier is needed per reflector. w: global scratch of m doubles.
+template <bool CL>
+__device__ void team_back_transform(Team<CL> &tm, int n, const double *A, const double *tau, double *Y,
+                                    int m, double *w, double *spart) {
+  const int j0 = (int)((int64_t)m * tm.rank / tm.size), j1 = (int)((int64_t)m * (tm.rank + 1) / tm.size);
+  const int mc = j1 - j0;
+  if (mc > 0) {
+    for (int k = n - 3; k >= 0; --k) {
+      const double t = ld<CL>(tau + k);
+      if (t == 0.0) continue;
+      const int mm = n - k - 1;
+      const double *col = A + (size_t)(k + 1) * n + k;
+      double *Yb = Y + (size_t)(k + 1) * m + j0;
+      // w_j = t * v . Y[:, j]; the r range split into G groups (all threads busy)
+      const int G = mc < (int)blockDim.x ? max(1, min(kPart / mc, (int)blockDim.x / mc)) : 1;
+      for (int q = threadIdx.x; q < G * mc; q += blockDim.x) {
+        const int j = q % mc, g = q / mc;
         double s = 0.0;
-        for (int g = 0; g < G; ++g) s += s_bpart[g * m + j];
-        w[j] = t * s;
+        for (int r = g; r < mm; r += G)
+          s = fma(r == 0 ? 1.0 : ld<CL>(col + (size_t)r * n), ld<CL>(Yb + (size_t)r * m + j), s);
+        if (G > 1) spart[g * mc + j] = s; else w[j0 + j] = t * s;
+      }
+      __syncthreads();
+      if (G > 1) {
+        for (int j = threadIdx.x; j < mc; j += blockDim.x) {
+          double s = 0.0;
+          for (int g = 0; g < G; ++g) s += spart[g * mc + j];
+          w[j0 + j] = t * s;
+        }
+        __syncthreads();
+      }
+      for (int64_t q = threadIdx.x; q < (int64_t)mm * mc; q += blockDim.x) {
+        const int r = (int)(q / mc), j = (int)(q % mc);
+        const double vr = r == 0 ? 1.0 : ld<CL>(col + (size_t)r * n);
+        Yb[(size_t)r * m + j] = ld<CL>(Yb + (size_t)r * m + j) - vr * w[j0 + j];
       }
       __syncthreads();
     }
-    for (int64_t q = threadIdx.x; q < (int64_t)mm * m; q += blockDim.x) {
-      const int r = (int)(q / m), j = (int)(q % m);
-      const double vr = r == 0 ? 1.0 : col[(size_t)r * n];
-      Yb[(size_t)r * m + j] -= vr * w[j];
-    }
-    __syncthreads();
   }
+  tm.sync();
 }
 
 }  // namespace dxtb

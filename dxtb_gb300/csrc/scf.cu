@@ -1,8 +1,11 @@
-// Persistent self-consistent-field kernel: one CTA per molecule runs the
-// whole SCF of that molecule (orthogonaliser, Fock build, generalized
-// eigensolve, Fermi occupations, density, Mulliken charges and atomic
-// multipoles, potentials, limited-memory Broyden root solve) with a
-// per-molecule convergence test and iteration cap. No host synchronisation inside the loop.
+// Persistent self-consistent-field kernels: a TEAM of CTAs runs the whole
+// SCF of one molecule (orthogonaliser, Fock build, generalized eigensolve,
+// Fermi occupations, density, Mulliken charges and atomic multipoles,
+// potentials, limited-memory Broyden root solve) with a per-molecule
+// convergence test and iteration cap. No host synchronisation inside the
+// loop. Small molecules run one 256-thread CTA each, two per SM; larger ones
+// one 512-thread CTA per SM; the largest a thread-block cluster of 2-16
+// CTAs (one SM each) that share every O(n^3) phase.
 //
 // Reference path (src/dxtb/_src): scf/iterator.py:51-195, scf/pure/
 // conversions.py:106-366 (charges <-> potential <-> Fock <-> density),
@@ -17,27 +20,31 @@
 namespace dxtb {
 
 constexpr int kScfThreads = 256;     // CTA size for molecules sharing an SM
-constexpr int kScfBigThreads = 512;  // CTA size for large molecules on their own SM
-constexpr int kRank = 256;        // Broyden inverse-Jacobian memory (the reference keeps all updates; >= maxiter)
-constexpr double kDamp = 0.5;     // step damping of the root solver (defaults.DAMP)
-constexpr int kSmemTri = 1024;    // tridiagonal copy in shared memory up to this order
-constexpr double kOccCut = 1e-15; // orbitals below this occupation carry no density
+constexpr int kScfBigThreads = 512;  // CTA size of one-SM and cluster teams
+constexpr int kRank = 256;           // Broyden memory (the reference keeps every update; >= maxiter)
+constexpr double kDamp = 0.5;        // step damping of the root solver (defaults.DAMP)
+constexpr double kOccCut = 1e-15;    // orbitals below this occupation carry no density
+constexpr int kLuSlots = 1024;       // concurrent inverse-iteration factorisations per molecule
+constexpr int kClasses = 6;          // size classes: 0 small, 1 one SM, 2..5 clusters of 2..16
+constexpr int kMaxCluster = 16;
 
 struct MolView {
   int m, n, nat, nsh, N;
   int64_t a0, s0, o0, moff, mtot, n2off, n2tot, g0;
 };
 
+__host__ __device__ inline int64_t lu_slots(int64_t n) { return n < kLuSlots ? n : kLuSlots; }
+
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * kScfBigThreads + n + 8 +
-         4 * kRank + 64;
+  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * lu_slots(n) + n + 8 +
+         4 * kRank + 64 + 64;
 }
 
 struct Ws {
   double *Linv, *A, *Zt, *d, *e, *tau, *p, *rc, *rs, *eps, *fa, *fb, *x, *g, *hx, *hr, *misc;
-  double *vsh_tmp, *lu, *sdot, *xold, *rold, *xbest;
+  double *vsh_tmp, *lu, *sdot, *xold, *rold, *xbest, *team;
   int *cl;
 };
 
@@ -65,9 +72,10 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.xold = q; q += N;
   w.rold = q; q += N;
   w.xbest = q; q += N;
-  w.lu = q; q += (size_t)5 * n * kScfBigThreads;
+  w.lu = q; q += (size_t)5 * n * lu_slots(n);
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
   w.sdot = q; q += 4 * kRank + 64;
+  w.team = q; q += 64;  // [0, 32) partial sums, [32, 48) broadcast words (int)
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
@@ -134,10 +142,21 @@ struct ScfArgs {
   const int32_t *order;
   double *ws, *P, *W, *C, *evals, *occ, *q, *dp, *qp, *vorb, *vdp, *vqp, *energies;
   int32_t *status;
+  int thr[kClasses];  // smallest n of each size class (thr[0] = 0)
 };
+
+// Size class of a molecule with n orbitals.
+__host__ __device__ inline int scf_class(const int *thr, int n) {
+  int c = 0;
+  for (int k = 1; k < kClasses; ++k)
+    if (n >= thr[k]) c = k;
+  return c;
+}
 
 // Potential x = (vorb [n], vdp [nat][3], vqp [nat][6]) from the orbital
 // charges qo and atomic multipoles dpa/qpa (interactions/base.py:135-181).
+// One CTA (the team's lead); qo, dpa, qpa may come from the whole team.
+template <bool CL>
 __device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, const double *qo,
                                        const double *dpa, const double *qpa, double *qsh,
                                        double *qat, double *vsh, double *vat, double *xout,
@@ -148,7 +167,7 @@ __device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, cons
     const int t = b.shell_type[mv.s0 + s];
     const int o = b.shell_ao[mv.s0 + s], no = 2 * pi_(a.pi, DXTB_I_L + t) + 1;
     double v = 0.0;
-    for (int k = 0; k < no; ++k) v += qo[o + k];
+    for (int k = 0; k < no; ++k) v += ld<CL>(qo + o + k);
     qsh[s] = v;
   }
   __syncthreads();
@@ -171,8 +190,8 @@ __device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, cons
     if (multipole) {
       for (int j = 0; j < nat; ++j) {
         const int64_t o = mv.n2off + (int64_t)i * nat + j;
-        for (int c = 0; c < 3; ++c) v += a.sd[c * mv.n2tot + o] * dpa[3 * j + c];
-        for (int c = 0; c < 6; ++c) v += a.sq[c * mv.n2tot + o] * qpa[6 * j + c];
+        for (int c = 0; c < 3; ++c) v += a.sd[c * mv.n2tot + o] * ld<CL>(dpa + 3 * j + c);
+        for (int c = 0; c < 6; ++c) v += a.sq[c * mv.n2tot + o] * ld<CL>(qpa + 6 * j + c);
       }
     }
     if (a.gb != nullptr) {
@@ -192,13 +211,13 @@ __device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, cons
       const int zj = b.numbers[mv.a0 + j];
       const double dk = pf(a.pf, DXTB_P_DKERNEL + zj), qk = pf(a.pf, DXTB_P_QKERNEL + zj);
       double vd[3], vq[6];
-      for (int c = 0; c < 3; ++c) vd[c] = 2.0 * dk * dpa[3 * j + c];
-      for (int c = 0; c < 6; ++c) vq[c] = 2.0 * qk * qpa[6 * j + c] * qscale[c];
+      for (int c = 0; c < 3; ++c) vd[c] = 2.0 * dk * ld<CL>(dpa + 3 * j + c);
+      for (int c = 0; c < 6; ++c) vq[c] = 2.0 * qk * ld<CL>(qpa + 6 * j + c) * qscale[c];
       for (int i = 0; i < nat; ++i) {
         const int64_t o = mv.n2off + (int64_t)i * nat + j;
         for (int c = 0; c < 3; ++c) vd[c] += a.sd[c * mv.n2tot + o] * qat[i];
         for (int x = 0; x < 3; ++x)
-          for (int y = 0; y < 3; ++y) vd[y] += a.dd[(3 * x + y) * mv.n2tot + o] * dpa[3 * i + x];
+          for (int y = 0; y < 3; ++y) vd[y] += a.dd[(3 * x + y) * mv.n2tot + o] * ld<CL>(dpa + 3 * i + x);
         for (int c = 0; c < 6; ++c) vq[c] += a.sq[c * mv.n2tot + o] * qat[i];
       }
       for (int c = 0; c < 3; ++c) xout[n + 3 * j + c] = vd[c];
@@ -208,7 +227,9 @@ __device__ void potential_from_charges(const ScfArgs &a, const MolView &mv, cons
   __syncthreads();
 }
 
-// Interaction energy (interactions/base.py:306-360 summed): block result.
+// Interaction energy (interactions/base.py:306-360 summed): block result of
+// the lead CTA.
+template <bool CL>
 __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const double *qsh,
                                      const double *qat, const double *dpa, const double *qpa,
                                      int multipole, int es3_shell, double *red) {
@@ -234,11 +255,17 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
         for (int c = 0; c < 3; ++c) vd[c] += a.sd[c * mv.n2tot + o] * qat[i];
         for (int x = 0; x < 3; ++x)
           for (int y = 0; y < 3; ++y)
-            vd[y] += 0.5 * a.dd[(3 * x + y) * mv.n2tot + o] * dpa[3 * i + x];
+            vd[y] += 0.5 * a.dd[(3 * x + y) * mv.n2tot + o] * ld<CL>(dpa + 3 * i + x);
         for (int c = 0; c < 6; ++c) vq[c] += a.sq[c * mv.n2tot + o] * qat[i];
       }
-      for (int c = 0; c < 3; ++c) e += (dk * dpa[3 * j + c] + vd[c]) * dpa[3 * j + c];
-      for (int c = 0; c < 6; ++c) e += (qk * qscale[c] * qpa[6 * j + c] + vq[c]) * qpa[6 * j + c];
+      for (int c = 0; c < 3; ++c) {
+        const double dj = ld<CL>(dpa + 3 * j + c);
+        e += (dk * dj + vd[c]) * dj;
+      }
+      for (int c = 0; c < 6; ++c) {
+        const double qj = ld<CL>(qpa + 6 * j + c);
+        e += (qk * qscale[c] * qj + vq[c]) * qj;
+      }
     }
     if (a.gb != nullptr) {
       const double *gr = a.gb + mv.n2off + (size_t)j * nat;
@@ -250,30 +277,133 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
   return block_sum(e, red);
 }
 
-// Molecules of at least kBigN orbitals among the first `nbig_max` of the
-// launch order run in a 512-thread CTA with an SM of their own; the others
-// share SMs two at a time in 256-thread CTAs. The two launches run
-// concurrently; every CTA checks which one its molecule belongs to.
-constexpr int kBigN = 128;
+// State of the root solver, held by the lead CTA only.
+struct Broyden {
+  int nrank = 0, final_eval = 0, hit_max = 0;
+  double resid = 0.0, best_ynorm = 1e308, dx_norm = 0.0;
+};
 
-__device__ __forceinline__ bool scf_is_big(const ScfArgs &a, int i, int nbig_max) {
-  const int m = a.order ? a.order[i] : i;
-  return i < nbig_max && (a.b.ao_off[m + 1] - a.b.ao_off[m]) >= kBigN;
+enum ScfAction : int { kNext = 0, kStop = 1 };
+
+// One step of the root solver on F(x) = x - G(x): limited-memory Broyden's
+// first method on the inverse Jacobian, Gm = 0.5 I + sum_k c_k d_k^T,
+// damped steps x += damp * dx, dx = -Gm F (the broyden1 of exlibs/xitorch/
+// _impls/optimize/root/{rootsolver.py:42-265, _jacobian.py:51-120} with
+// alpha = -0.5, damp = 0.5, line_search = False, scf/base.py:267-292);
+// stop when |dx|_2 < x_tol and |F|_2 < f_tol. Lead CTA only.
+__device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br, int &status,
+                            double *red) {
+  double *sdot = w.sdot;         // [kRank] dot products
+  double *sdot2 = sdot + kRank;  // [kRank]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (int)(blockDim.x >> 5);
+  // |F|^2 with F = x - G(x)
+  double part = 0.0;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    const double y = w.x[t] - w.g[t];
+    part += y * y;
+  }
+  const double ynorm = sqrt(block_sum(part, red));
+  br.resid = ynorm;
+  if (it == 1) {
+    if (ynorm <= a.ftol * kEps) return kStop;
+    br.nrank = 0;
+  } else {
+    if (ynorm < br.best_ynorm) {
+      br.best_ynorm = ynorm;
+      for (int t = threadIdx.x; t < N; t += blockDim.x) w.xbest[t] = w.x[t];
+    }
+    // Broyden update with dx = x - x_prev, dy = F - F_prev:
+    // v = Gm^T dx, c = dx - Gm dy, d = v / (dy . v)
+    if (br.nrank >= kRank) br.nrank = 0;  // "restart" reduction of a full memory (not reached: kRank >= maxiter)
+    const int nrank = br.nrank;
+    for (int k = wid; k < 2 * nrank; k += nw) {
+      const int kk = k >> 1;
+      double s = 0.0;
+      if ((k & 1) == 0) {
+        const double *ck = w.hx + (size_t)kk * N;
+        for (int t = lane; t < N; t += 32) s += ck[t] * (w.x[t] - w.xold[t]);
+      } else {
+        const double *dk = w.hr + (size_t)kk * N;
+        for (int t = lane; t < N; t += 32) s += dk[t] * ((w.x[t] - w.g[t]) - w.rold[t]);
+      }
+      s = warp_sum(s);
+      if (lane == 0) {
+        if ((k & 1) == 0) sdot[kk] = s; else sdot2[kk] = s;
+      }
+    }
+    __syncthreads();
+    double *cn = w.hx + (size_t)nrank * N, *dn = w.hr + (size_t)nrank * N;
+    double pdv = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      const double dxt = w.x[t] - w.xold[t];
+      const double dyt = (w.x[t] - w.g[t]) - w.rold[t];
+      double v = 0.5 * dxt, gdy = 0.5 * dyt;
+      for (int k = 0; k < nrank; ++k) {
+        v += w.hr[(size_t)k * N + t] * sdot[k];
+        gdy += w.hx[(size_t)k * N + t] * sdot2[k];
+      }
+      cn[t] = dxt - gdy;
+      dn[t] = v;
+      pdv += dyt * v;
+    }
+    const double dyv = block_sum(pdv, red);
+    if (dyv == 0.0 || !isfinite(dyv)) {
+      status = DXTB_ERR_NAN;
+      return kStop;
+    }
+    const double idyv = 1.0 / dyv;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) dn[t] *= idyv;
+    ++br.nrank;
+    __syncthreads();
+    if (br.dx_norm < a.xtol && ynorm < a.ftol) return kStop;  // converged at x
+  }
+  if (it >= a.maxiter) {
+    // not converged: evaluate once more at the best iterate, which the root
+    // solver returns with a warning (rootsolver.py:250-259)
+    if (br.best_ynorm < ynorm) {
+      for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = w.xbest[t];
+      br.final_eval = 1;
+      __syncthreads();
+      return kNext;
+    }
+    br.hit_max = 1;
+    return kStop;
+  }
+  // F_prev = F, x_prev = x; dx = -Gm F = -(0.5 F + sum_k c_k (d_k . F))
+  const int nrank = br.nrank;
+  for (int k = wid; k < nrank; k += nw) {
+    const double *dk = w.hr + (size_t)k * N;
+    double s = 0.0;
+    for (int t = lane; t < N; t += 32) s += dk[t] * (w.x[t] - w.g[t]);
+    s = warp_sum(s);
+    if (lane == 0) sdot[k] = s;
+  }
+  __syncthreads();
+  double pdx = 0.0;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    const double y = w.x[t] - w.g[t];
+    double dx = -0.5 * y;
+    for (int k = 0; k < nrank; ++k) dx -= w.hx[(size_t)k * N + t] * sdot[k];
+    w.rold[t] = y;
+    w.xold[t] = w.x[t];
+    w.x[t] += kDamp * dx;
+    pdx += dx * dx;
+  }
+  br.dx_norm = sqrt(block_sum(pdx, red));
+  if (br.dx_norm == 0.0) {
+    status = DXTB_ERR_NAN;
+    return kStop;
+  }
+  return kNext;
 }
 
-__device__ __forceinline__ void scf_body(const ScfArgs &a, int m);
-
-template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) k_scf(ScfArgs a, int big, int nbig_max) {
-  const int i = blockIdx.x;
-  if (scf_is_big(a, i, nbig_max) != (big != 0)) return;
-  scf_body(a, a.order ? a.order[i] : i);
-}
-
-__device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
+// The SCF of molecule m_ by the team tm. dsm: dynamic shared memory of
+// 3 n doubles + 2 n floats (n of this molecule or larger).
+template <bool CL>
+__device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
   __shared__ double red[32];
-  __shared__ int s_flag, s_m, s_ncl;
-  __shared__ double s_tri[2 * kSmemTri];
+  __shared__ double spart[kPart];
   const dxtb_batch &b = a.b;
   MolView mv;
   mv.m = m_;
@@ -295,9 +425,15 @@ __device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
   const int N = n + (multipole ? 9 * nat : 0);
   mv.N = N;
   Ws w = ws_carve(a.ws + a.ws_off[m], n, nat);
+  tm.gred = w.team;
+  tm.gctl = reinterpret_cast<int *>(w.team + 32);
+  tm.phase = 0;
   double *qsh = w.misc, *qat = qsh + mv.nsh + 1, *vat = qat + nat + 1;
   double *dpa = vat + nat + 1, *qpa = dpa + 3 * nat + 1, *qo = qpa + 6 * nat + 1;
   double *vsh = w.vsh_tmp;
+  // shared copies: tridiagonal (sd, se), sorted eigenvalues (sw), float32 (df, e2f)
+  double *sd = dsm, *se = dsm + n, *sw = dsm + 2 * n;
+  float *df = reinterpret_cast<float *>(dsm + 3 * n), *e2f = df + n;
 
   const double *S = a.S + mv.moff, *H0 = a.H0 + mv.moff;
   double *P = a.P + mv.moff, *C = a.C + mv.moff;
@@ -306,118 +442,116 @@ __device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
   int status = DXTB_OK;
 
   // ---- orthogonaliser X = L^-1 (S = L L^T), once per geometry ----
-  for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) w.A[t] = S[t];
-  __syncthreads();
-  if (!cta_cholesky(n, w.A)) status = DXTB_ERR_NOT_POSDEF;
-  if (status == DXTB_OK) cta_trinv(n, w.A, w.Linv);
+  for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) w.A[t] = S[t];
+  tm.sync();
+  if (!team_cholesky(tm, n, w.A)) status = DXTB_ERR_NOT_POSDEF;
+  if (status == DXTB_OK) team_trinv(tm, n, w.A, w.Linv);
+  for (int t = tm.tid; t < N; t += tm.nthr) w.x[t] = 0.0;
+  tm.sync();
 
-  for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = 0.0;
-  __syncthreads();
-
-  int it = 0, nrank = 0, final_eval = 0, hit_max = 0;
-  double resid = 0.0, best_ynorm = 1e308, dx_norm = 0.0;
+  int it = 0, mo = 1;
+  Broyden br;
   while (status == DXTB_OK) {
     ++it;
     // ---- Fock matrix F(x) into Zt (conversions.py:255-297) ----
-    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+    for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
       const int i = (int)(t / n), j = (int)(t % n);
-      double f = H0[t] - 0.5 * S[t] * (w.x[i] + w.x[j]);
+      double f = H0[t] - 0.5 * S[t] * (ld<CL>(w.x + i) + ld<CL>(w.x + j));
       if (multipole) {
         const int ai = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + i]];
         const int aj = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + j]];
         const int64_t e1 = mv.moff + t, e2 = mv.moff + (int64_t)j * n + i;
         double acc = 0.0;
         for (int c = 0; c < 3; ++c)
-          acc += a.D[c * mv.mtot + e1] * w.x[n + 3 * aj + c] + a.D[c * mv.mtot + e2] * w.x[n + 3 * ai + c];
+          acc += a.D[c * mv.mtot + e1] * ld<CL>(w.x + n + 3 * aj + c) +
+                 a.D[c * mv.mtot + e2] * ld<CL>(w.x + n + 3 * ai + c);
         for (int c = 0; c < 6; ++c)
-          acc += a.Q[c * mv.mtot + e1] * w.x[n + 3 * nat + 6 * aj + c] +
-                 a.Q[c * mv.mtot + e2] * w.x[n + 3 * nat + 6 * ai + c];
+          acc += a.Q[c * mv.mtot + e1] * ld<CL>(w.x + n + 3 * nat + 6 * aj + c) +
+                 a.Q[c * mv.mtot + e2] * ld<CL>(w.x + n + 3 * nat + 6 * ai + c);
         f -= 0.5 * acc;
       }
       w.Zt[t] = f;
     }
-    __syncthreads();
+    tm.sync();
     // ---- F' = X F X^T (exlibs/xitorch/_impls/linalg/symeig.py:57-61) ----
     // X = L^-1 is lower triangular: A = X F needs k <= i; only the lower
     // triangle of (X F) X^T is formed (k <= j), then mirrored.
-    cta_gemm<false, false>(n, n, n, 1.0, w.Linv, n, w.Zt, n, 0.0, w.A, n, kALower);
-    cta_gemm<false, true>(n, n, n, 1.0, w.A, n, w.Linv, n, 0.0, w.Zt, n, kBLowerT, true);
-    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+    team_gemm<false, false>(tm, n, n, n, 1.0, w.Linv, n, w.Zt, n, 0.0, w.A, n, kALower);
+    team_gemm<false, true>(tm, n, n, n, 1.0, w.A, n, w.Linv, n, 0.0, w.Zt, n, kBLowerT, true);
+    for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
       const int i = (int)(t / n), j = (int)(t % n);
-      w.A[t] = j <= i ? w.Zt[t] : w.Zt[(size_t)j * n + i];
+      w.A[t] = j <= i ? ld<CL>(w.Zt + t) : ld<CL>(w.Zt + (size_t)j * n + i);
+    }
+    tm.sync();
+    // ---- eigenvalues: Householder tridiagonalisation + bisection/Newton ----
+    team_tridiag(tm, n, w.A, w.d, w.e, w.tau, w.p, sd, se, spart, red);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      sd[i] = ld<CL>(w.d + i);
+      se[i] = ld<CL>(w.e + i);
     }
     __syncthreads();
-    // ---- eigenvalues: Householder tridiagonalisation + implicit QL ----
-    cta_tridiag(n, w.A, w.d, w.e, w.tau, w.p, w.rs, red);
-    {
-      float *df = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) : reinterpret_cast<float *>(w.rs);
-      float *e2f = n <= 2 * kSmemTri ? reinterpret_cast<float *>(s_tri) + 2 * kSmemTri
-                                     : reinterpret_cast<float *>(w.vsh_tmp);
-      cta_tri_eigenvalues(n, w.d, w.e, w.rc, df, e2f);
-    }
-    cta_rank_sort(n, w.rc, w.eps);  // ascending, like eigh
+    team_tri_eigenvalues(tm, n, sd, se, sw, w.rc, df, e2f);  // sw: e^2 scratch here
+    team_rank_sort(tm, n, w.rc, w.eps, sw);  // ascending, like eigh
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sw[i] = ld<CL>(w.eps + i);
+    double tnorm = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) tnorm = fmax(tnorm, fabs(sd[j]) + 2.0 * fabs(se[j]));
+    tnorm = block_max(tnorm, red);  // also orders the sw writes
     // ---- Fermi occupations (filling.py:428-742), both spin channels ----
-    if (threadIdx.x < 32) {
-      bool ok = fermi_warp(n, w.eps, nel_a, a.kt, w.fa);
+    if (tm.lead() && threadIdx.x < 32) {
+      bool ok = fermi_warp(n, sw, nel_a, a.kt, w.fa);
       if (nel_b == nel_a) {
         for (int j = threadIdx.x; j < n; j += 32) w.fb[j] = w.fa[j];
       } else {
-        ok = ok && fermi_warp(n, w.eps, nel_b, a.kt, w.fb);
+        ok = ok && fermi_warp(n, sw, nel_b, a.kt, w.fb);
       }
       __syncwarp();
       if (threadIdx.x == 0) {
-        s_flag = ok ? 1 : 0;
-        // orbitals with non-vanishing occupation (occupations decrease with j)
-        int mv_ = 0;
-        while (mv_ < n && w.fa[mv_] + w.fb[mv_] > kOccCut) ++mv_;
-        s_m = mv_ > 0 ? mv_ : 1;
+        // orbitals with non-vanishing occupation (occupations decrease with
+        // j), extended to the end of their eigenvalue cluster
+        int mm = 0;
+        while (mm < n && w.fa[mm] + w.fb[mm] > kOccCut) ++mm;
+        mm = mm > 0 ? mm : 1;
+        const double ctol = 1e-6 * fmax(tnorm, 1.0);
+        while (mm < n && sw[mm] - sw[mm - 1] <= ctol) ++mm;
+        tm.gctl[0] = ok ? 1 : 0;
+        tm.gctl[1] = mm;
       }
     }
-    __syncthreads();
-    if (!s_flag) {
+    tm.sync();
+    if (!ldi<CL>(tm.gctl + 0)) {
       status = DXTB_ERR_FERMI;
       break;
     }
-    // ---- eigenvectors of the m lowest orbitals only ----
-    double tnorm = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) tnorm = fmax(tnorm, fabs(w.d[j]) + 2.0 * fabs(w.e[j]));
-    tnorm = block_max(tnorm, red);
-    if (threadIdx.x == 0) {
-      // keep a whole eigenvalue cluster together
-      int mm = s_m;
-      const double ctol = 1e-6 * fmax(tnorm, 1.0);
-      while (mm < n && w.eps[mm] - w.eps[mm - 1] <= ctol) ++mm;
-      s_m = mm;
-    }
-    __syncthreads();
-    const int mo = s_m;
-    cta_tri_vectors(n, w.d, w.e, w.eps, mo, tnorm, w.Zt, w.lu, w.cl, &s_ncl);
-    cta_back_transform(n, w.A, w.tau, w.Zt, mo, w.p);
+    mo = ldi<CL>(tm.gctl + 1);
+    // ---- eigenvectors of the mo lowest orbitals only ----
+    team_tri_vectors(tm, n, sd, se, sw, mo, tnorm, w.Zt, w.lu, (int)min((int64_t)tm.nthr, lu_slots(n)), w.cl);
+    team_back_transform(tm, n, w.A, w.tau, w.Zt, mo, w.p, spart);
     // ---- C^T = Y^T X (orbital j is row j; X lower -> k >= i) ----
-    cta_gemm<true, false>(mo, n, n, 1.0, w.Zt, mo, w.Linv, n, 0.0, C, n, kBUpper);
-    for (int j = threadIdx.x; j < n; j += blockDim.x) w.p[j] = w.fa[j] + w.fb[j];
-    __syncthreads();
+    team_gemm<true, false>(tm, mo, n, n, 1.0, w.Zt, mo, w.Linv, n, 0.0, C, n, kBUpper);
     // ---- density P = C diag(occ) C^T (scf/utils.py:29-52) ----
-    for (int64_t t = threadIdx.x; t < (int64_t)mo * n; t += blockDim.x) w.A[t] = C[t] * w.p[t / n];
-    __syncthreads();
-    cta_gemm<true, false>(n, n, mo, 1.0, C, n, w.A, n, 0.0, P, n, kFull, true);
-    cta_mirror_lower(n, P);
+    for (int64_t t = tm.tid; t < (int64_t)mo * n; t += tm.nthr) {
+      const int j = (int)(t / n);
+      w.A[t] = ld<CL>(C + t) * (ld<CL>(w.fa + j) + ld<CL>(w.fb + j));
+    }
+    tm.sync();
+    team_gemm<true, false>(tm, n, n, mo, 1.0, C, n, w.A, n, 0.0, P, n, kFull, true);
+    team_mirror_lower(tm, n, P);
     // ---- Mulliken charges and atomic multipoles (conversions.py:203-251) ----
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = tm.tid; i < n; i += tm.nthr) {
       double pop = 0.0;
-      for (int k = 0; k < n; ++k) pop = fma(P[(size_t)k * n + i], S[(size_t)k * n + i], pop);
+      for (int k = 0; k < n; ++k) pop = fma(ld<CL>(P + (size_t)k * n + i), S[(size_t)k * n + i], pop);
       qo[i] = n0[i] - pop;
     }
     if (multipole) {
-      for (int t = threadIdx.x; t < 3 * nat; t += blockDim.x) dpa[t] = 0.0;
-      for (int t = threadIdx.x; t < 6 * nat; t += blockDim.x) qpa[t] = 0.0;
-      __syncthreads();
+      for (int t = tm.tid; t < 3 * nat; t += tm.nthr) dpa[t] = 0.0;
+      for (int t = tm.tid; t < 6 * nat; t += tm.nthr) qpa[t] = 0.0;
+      tm.sync();
       // -sum_k P_ik M[c][k][i] per orbital i, reduced onto the atom of i
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      for (int i = tm.tid; i < n; i += tm.nthr) {
         double acc[9];
         for (int c = 0; c < 9; ++c) acc[c] = 0.0;
         for (int k = 0; k < n; ++k) {
-          const double pk = P[(size_t)k * n + i];
+          const double pk = ld<CL>(P + (size_t)k * n + i);
           const int64_t e = mv.moff + (int64_t)k * n + i;
           for (int c = 0; c < 3; ++c) acc[c] -= pk * a.D[c * mv.mtot + e];
           for (int c = 0; c < 6; ++c) acc[3 + c] -= pk * a.Q[c * mv.mtot + e];
@@ -427,172 +561,116 @@ __device__ __forceinline__ void scf_body(const ScfArgs &a, int m_) {
         for (int c = 0; c < 6; ++c) atomicAdd(&qpa[6 * ai + c], acc[3 + c]);
       }
     }
-    __syncthreads();
-    // ---- new potential G(x) ----
-    potential_from_charges(a, mv, qo, dpa, qpa, qsh, qat, vsh, vat, w.g, multipole, es3_shell);
-    if (final_eval) {
-      hit_max = 1;
-      break;
-    }
-    // ---- root solver on F(x) = x - G(x): limited-memory Broyden's first
-    // method on the inverse Jacobian, Gm = 0.5 I + sum_k c_k d_k^T, damped
-    // steps x += damp * dx, dx = -Gm F (the broyden1 of exlibs/xitorch/
-    // _impls/optimize/root/{rootsolver.py:42-265, _jacobian.py:51-120} with
-    // alpha = -0.5, damp = 0.5, line_search = False, scf/base.py:267-292);
-    // stop when |dx|_2 < x_tol and |F|_2 < f_tol. ----
-    {
-      double *sdot = w.sdot;                     // [kRank] dot products
-      double *sdot2 = sdot + kRank;              // [kRank]
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      const int nw = (int)(blockDim.x >> 5);
-      // |F|^2 with F = x - G(x)
-      double part = 0.0;
-      for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        const double y = w.x[t] - w.g[t];
-        part += y * y;
-      }
-      const double ynorm = sqrt(block_sum(part, red));
-      resid = ynorm;
-      if (it == 1) {
-        if (ynorm <= a.ftol * kEps) break;
-        nrank = 0;
+    tm.sync();
+    // ---- new potential G(x) and the root-solver step (lead CTA) ----
+    if (tm.lead()) {
+      potential_from_charges<CL>(a, mv, qo, dpa, qpa, qsh, qat, vsh, vat, w.g, multipole, es3_shell);
+      int act;
+      if (br.final_eval) {
+        br.hit_max = 1;
+        act = kStop;
       } else {
-        if (ynorm < best_ynorm) {
-          best_ynorm = ynorm;
-          for (int t = threadIdx.x; t < N; t += blockDim.x) w.xbest[t] = w.x[t];
-        }
-        // Broyden update with dx = x - x_prev, dy = F - F_prev:
-        // v = Gm^T dx, c = dx - Gm dy, d = v / (dy . v)
-        if (nrank >= kRank) nrank = 0;  // "restart" reduction of a full memory
-        for (int k = wid; k < 2 * nrank; k += nw) {
-          const int kk = k >> 1;
-          double s = 0.0;
-          if ((k & 1) == 0) {
-            const double *ck = w.hx + (size_t)kk * N;
-            for (int t = lane; t < N; t += 32) s += ck[t] * (w.x[t] - w.xold[t]);
-          } else {
-            const double *dk = w.hr + (size_t)kk * N;
-            for (int t = lane; t < N; t += 32) s += dk[t] * ((w.x[t] - w.g[t]) - w.rold[t]);
-          }
-          s = warp_sum(s);
-          if (lane == 0) {
-            if ((k & 1) == 0) sdot[kk] = s; else sdot2[kk] = s;
-          }
-        }
-        __syncthreads();
-        double *cn = w.hx + (size_t)nrank * N, *dn = w.hr + (size_t)nrank * N;
-        double pdv = 0.0;
-        for (int t = threadIdx.x; t < N; t += blockDim.x) {
-          const double dxt = w.x[t] - w.xold[t];
-          const double dyt = (w.x[t] - w.g[t]) - w.rold[t];
-          double v = 0.5 * dxt, gdy = 0.5 * dyt;
-          for (int k = 0; k < nrank; ++k) {
-            v += w.hr[(size_t)k * N + t] * sdot[k];
-            gdy += w.hx[(size_t)k * N + t] * sdot2[k];
-          }
-          cn[t] = dxt - gdy;
-          dn[t] = v;
-          pdv += dyt * v;
-        }
-        const double dyv = block_sum(pdv, red);
-        if (dyv == 0.0 || !isfinite(dyv)) {
-          status = DXTB_ERR_NAN;
-          break;
-        }
-        const double idyv = 1.0 / dyv;
-        for (int t = threadIdx.x; t < N; t += blockDim.x) dn[t] *= idyv;
-        ++nrank;
-        __syncthreads();
-        if (dx_norm < a.xtol && ynorm < a.ftol) break;  // converged at x
+        act = broyden_step(a, w, N, it, br, status, red);
       }
-      if (it >= a.maxiter) {
-        // not converged: evaluate once more at the best iterate, which the
-        // root solver returns with a warning (rootsolver.py:250-259)
-        if (best_ynorm < ynorm) {
-          for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = w.xbest[t];
-          final_eval = 1;
-          __syncthreads();
-          continue;
-        }
-        hit_max = 1;
-        break;
-      }
-      // F_prev = F, x_prev = x; dx = -Gm F = -(0.5 F + sum_k c_k (d_k . F))
-      for (int k = wid; k < nrank; k += nw) {
-        const double *dk = w.hr + (size_t)k * N;
-        double s = 0.0;
-        for (int t = lane; t < N; t += 32) s += dk[t] * (w.x[t] - w.g[t]);
-        s = warp_sum(s);
-        if (lane == 0) sdot[k] = s;
-      }
-      __syncthreads();
-      double pdx = 0.0;
-      for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        const double y = w.x[t] - w.g[t];
-        double dx = -0.5 * y;
-        for (int k = 0; k < nrank; ++k) dx -= w.hx[(size_t)k * N + t] * sdot[k];
-        w.rold[t] = y;
-        w.xold[t] = w.x[t];
-        w.x[t] += kDamp * dx;
-        pdx += dx * dx;
-      }
-      dx_norm = sqrt(block_sum(pdx, red));
-      if (dx_norm == 0.0) {
-        status = DXTB_ERR_NAN;
-        break;
+      if (threadIdx.x == 0) {
+        tm.gctl[3] = act;
+        tm.gctl[4] = (act == kStop && br.hit_max && status == DXTB_OK) ? DXTB_ERR_MAXITER : status;
       }
     }
-    __syncthreads();
+    tm.sync();
+    status = ldi<CL>(tm.gctl + 4);
+    if (ldi<CL>(tm.gctl + 3) == kStop) break;
   }
-  if (hit_max && status == DXTB_OK) status = DXTB_ERR_MAXITER;
 
   // ---- outputs ----
   if (status == DXTB_OK || status == DXTB_ERR_MAXITER) {
     // energies (scf/base.py:510-619): E_h0 + E_int and -TS
     double part = 0.0;
-    for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) part += P[t] * H0[t];
-    const double eh0 = block_sum(part, red);
-    const double eint = interaction_energy(a, mv, qsh, qat, dpa, qpa, multipole, es3_shell, red);
-    double ts = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) ts += ent(w.fa[j]) + ent(w.fb[j]);
-    ts = a.kt * block_sum(ts, red);
-    if (threadIdx.x == 0) {
-      a.energies[4 * m + 0] = eh0 + eint;
-      a.energies[4 * m + 1] = ts;
-      a.energies[4 * m + 2] = (double)it;
-      a.energies[4 * m + 3] = resid;
-      if (!isfinite(eh0 + eint + ts)) status = DXTB_ERR_NAN;
-    }
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      a.evals[mv.o0 + j] = w.eps[j];
-      a.occ[mv.o0 + j] = w.fa[j] + w.fb[j];
-      a.q[mv.o0 + j] = qo[j];
-    }
-    // potentials of the final charges (for the gradient)
-    for (int t = threadIdx.x; t < n; t += blockDim.x) a.vorb[mv.o0 + t] = w.g[t];
-    if (multipole) {
-      for (int t = threadIdx.x; t < 3 * nat; t += blockDim.x) {
-        a.vdp[3 * mv.a0 + t] = w.g[n + t];
-        a.dp[3 * mv.a0 + t] = dpa[t];
+    for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) part += ld<CL>(P + t) * H0[t];
+    const double eh0 = team_sum(tm, part, red);
+    if (tm.lead()) {
+      const double eint = interaction_energy<CL>(a, mv, qsh, qat, dpa, qpa, multipole, es3_shell, red);
+      double ts = 0.0;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) ts += ent(w.fa[j]) + ent(w.fb[j]);
+      ts = a.kt * block_sum(ts, red);
+      if (threadIdx.x == 0) {
+        a.energies[4 * m + 0] = eh0 + eint;
+        a.energies[4 * m + 1] = ts;
+        a.energies[4 * m + 2] = (double)it;
+        a.energies[4 * m + 3] = br.resid;
+        if (!isfinite(eh0 + eint + ts)) status = DXTB_ERR_NAN;
       }
-      for (int t = threadIdx.x; t < 6 * nat; t += blockDim.x) {
-        a.vqp[6 * mv.a0 + t] = w.g[n + 3 * nat + t];
-        a.qp[6 * mv.a0 + t] = qpa[t];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        a.evals[mv.o0 + j] = sw[j];
+        a.occ[mv.o0 + j] = w.fa[j] + w.fb[j];
+        a.q[mv.o0 + j] = ld<CL>(qo + j);
+      }
+      // potentials of the final charges (for the gradient)
+      for (int t = threadIdx.x; t < n; t += blockDim.x) a.vorb[mv.o0 + t] = w.g[t];
+      if (multipole) {
+        for (int t = threadIdx.x; t < 3 * nat; t += blockDim.x) {
+          a.vdp[3 * mv.a0 + t] = w.g[n + t];
+          a.dp[3 * mv.a0 + t] = ld<CL>(dpa + t);
+        }
+        for (int t = threadIdx.x; t < 6 * nat; t += blockDim.x) {
+          a.vqp[6 * mv.a0 + t] = w.g[n + 3 * nat + t];
+          a.qp[6 * mv.a0 + t] = ld<CL>(qpa + t);
+        }
       }
     }
-    // energy-weighted density W = C diag(occ eps) C^T over the m orbitals
-    const int mo = s_m;
+    // energy-weighted density W = C diag(occ eps) C^T over the mo orbitals
     if (a.W != nullptr) {
-      for (int64_t t = threadIdx.x; t < (int64_t)mo * n; t += blockDim.x)
-        w.A[t] = C[t] * (w.fa[t / n] + w.fb[t / n]) * w.eps[t / n];
-      __syncthreads();
-      cta_gemm<true, false>(n, n, mo, 1.0, C, n, w.A, n, 0.0, a.W + mv.moff, n, kFull, true);
-      cta_mirror_lower(n, a.W + mv.moff);
+      for (int64_t t = tm.tid; t < (int64_t)mo * n; t += tm.nthr) {
+        const int j = (int)(t / n);
+        w.A[t] = ld<CL>(C + t) * (ld<CL>(w.fa + j) + ld<CL>(w.fb + j)) * sw[j];
+      }
+      tm.sync();
+      team_gemm<true, false>(tm, n, n, mo, 1.0, C, n, w.A, n, 0.0, a.W + mv.moff, n, kFull, true);
+      team_mirror_lower(tm, n, a.W + mv.moff);
     }
     // coefficients of orbitals without occupation are not computed
-    for (int64_t t = (int64_t)mo * n + threadIdx.x; t < (int64_t)n * n; t += blockDim.x) C[t] = 0.0;
+    for (int64_t t = (int64_t)mo * n + tm.tid; t < (int64_t)n * n; t += tm.nthr) C[t] = 0.0;
   }
-  if (threadIdx.x == 0) a.status[m] = status;
+  if (tm.lead() && threadIdx.x == 0) a.status[m] = status;
+  tm.sync();  // the team's workspace may be reused by its next molecule
+}
+
+// One CTA per molecule of size class `cls` (0: NT = 256, two per SM;
+// 1: NT = 512, one per SM); CTA i takes the i-th molecule of the launch order.
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_scf(ScfArgs a, int cls) {
+  extern __shared__ double dsm[];
+  const int i = blockIdx.x;
+  const int m = a.order ? a.order[i] : i;
+  if (scf_class(a.thr, (int)(a.b.ao_off[m + 1] - a.b.ao_off[m])) != cls) return;
+  Team<false> tm;
+  tm.rank = 0;
+  tm.size = 1;
+  tm.tid = threadIdx.x;
+  tm.stid = threadIdx.x;
+  tm.nthr = blockDim.x;
+  scf_body<false>(a, m, tm, dsm);
+}
+
+// One thread-block cluster per molecule of size class `cls` (2..5); the
+// clusters of the launch take the molecules of the class in launch order,
+// round robin. Every CTA of a cluster walks the same list, so the team's
+// control flow is uniform.
+__global__ void __launch_bounds__(kScfBigThreads, 1) k_scf_cluster(ScfArgs a, int cls) {
+  extern __shared__ double dsm[];
+  Team<true> tm;
+  tm.rank = (int)cluster_ctarank();
+  tm.size = (int)cluster_nctarank();
+  tm.tid = tm.rank * blockDim.x + threadIdx.x;
+  tm.stid = threadIdx.x * tm.size + tm.rank;
+  tm.nthr = tm.size * blockDim.x;
+  const int q = blockIdx.x / tm.size, nq = gridDim.x / tm.size;
+  int cnt = 0;
+  for (int i = 0; i < a.b.nmol; ++i) {
+    const int m = a.order ? a.order[i] : i;
+    if (scf_class(a.thr, (int)(a.b.ao_off[m + 1] - a.b.ao_off[m])) != cls) continue;
+    if (cnt++ % nq == q) scf_body<true>(a, m, tm, dsm);
+  }
 }
 
 }  // namespace dxtb
@@ -605,21 +683,25 @@ extern "C" int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat) { return ws_si
 
 namespace dxtb {
 
-// Side stream and fork/join events per (device, caller stream), created once
-// (no device memory is allocated); both launches stay inside a caller's
+// Size-class thresholds (smallest n of classes 1..5), process-wide.
+static std::mutex g_policy_mutex;
+static int g_thr[kClasses] = {0, 128, 144, 192, 320, 640};
+
+// Side streams and fork/join events per (device, caller stream), created once
+// (no device memory is allocated); all launches stay inside a caller's
 // stream capture. Callers on different streams (the serving loop's slots)
 // get different side streams, so their large-molecule kernels overlap.
 struct SideStream {
   cudaStream_t caller = nullptr;
-  cudaStream_t s = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t s[kClasses] = {};
+  cudaEvent_t fork = nullptr, join[kClasses] = {};
   bool used = false;
 };
 constexpr int kSidePerDev = 32;
 static std::mutex g_side_mutex;
 static SideStream g_side[64][kSidePerDev];
 
-// nullptr (and DXTB_OK) when the table is full: both launches then go to
+// nullptr (and DXTB_OK) when the table is full: all launches then go to
 // the caller's stream, one after the other.
 static int32_t side_stream(cudaStream_t caller, SideStream **out) {
   *out = nullptr;
@@ -636,40 +718,145 @@ static int32_t side_stream(cudaStream_t caller, SideStream **out) {
     if (!ss.used && slot == nullptr) slot = &ss;
   }
   if (slot == nullptr) return DXTB_OK;
-  if (cudaStreamCreateWithFlags(&slot->s, cudaStreamNonBlocking) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  // the larger classes run on the highest-priority streams: their CTAs need
+  // whole SMs and bound the batch's makespan, so they are dispatched first
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  for (int c = 0; c < kClasses; ++c) {
+    const int prio = max(greatest, least - c);  // class 0: the lowest priority
+    if (cudaStreamCreateWithPriority(&slot->s[c], cudaStreamNonBlocking, prio) != cudaSuccess)
+      return DXTB_ERR_LAUNCH;
+    if (cudaEventCreateWithFlags(&slot->join[c], cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  }
   if (cudaEventCreateWithFlags(&slot->fork, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
-  if (cudaEventCreateWithFlags(&slot->join, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
   slot->caller = caller;
   slot->used = true;
   *out = slot;
   return DXTB_OK;
 }
 
-static int32_t launch_scf(const ScfArgs &a, int nmol, cudaStream_t st) {
+// Largest usable cluster size of k_scf_cluster with `smem` bytes of dynamic
+// shared memory (cached per device and shared-memory size).
+static int cluster_cap(size_t smem) {
+  static std::mutex mu;
+  static int cap_dev[64] = {0};
+  static size_t cap_smem[64] = {0};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (cap_dev[dev] != 0 && cap_smem[dev] >= smem) return cap_dev[dev];
+  if (cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  int cap = 1;
+  for (int c = 2; c <= kMaxCluster; c *= 2) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(kScfBigThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_scf_cluster, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      break;
+    }
+    cap = c;
+  }
+  cap_dev[dev] = cap;
+  cap_smem[dev] = smem;
+  return cap;
+}
+
+static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
+  {
+    std::lock_guard<std::mutex> lock(g_policy_mutex);
+    for (int c = 0; c < kClasses; ++c) a.thr[c] = g_thr[c];
+  }
+  int sms = 0;
+  if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
+  const int nmax = a.b.max_nao;
+  const size_t smem = (size_t)nmax * (3 * sizeof(double) + 2 * sizeof(float));
+  if (smem > 200 * 1024) return DXTB_ERR_TOO_LARGE;
+  // clusters need the launch order; classes beyond the cluster cap fold down
+  int top = a.order ? 5 : 1;
+  if (top > 1 && scf_class(a.thr, nmax) >= 2) {
+    const int cap = cluster_cap(smem);
+    int c = 1;
+    while ((2 << (c - 1)) <= cap && c < 5) ++c;  // largest class whose cluster fits
+    top = cap >= 2 ? c : 1;
+  }
+  for (int c = top + 1; c < kClasses; ++c) a.thr[c] = INT32_MAX;
+  const int cmax = scf_class(a.thr, nmax);
   SideStream *ss = nullptr;
   int32_t rc = side_stream(st, &ss);
   if (rc != DXTB_OK) return rc;
-  int sms = 0;
-  if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
-  const int nbig_max = min(nmol, sms / 2);
-  // big molecules on the side stream, the rest on the caller's stream
-  cudaStream_t sb = ss ? ss->s : st;
+  // every class waits for the same fork event on its own stream, so all
+  // become ready together and the stream priorities order the dispatch (a
+  // CTA of class >= 1 needs a whole SM: it must not queue behind the
+  // two-per-SM CTAs that would otherwise spread over every SM first)
   if (ss) {
     if (cudaEventRecord(ss->fork, st) != cudaSuccess) return DXTB_ERR_LAUNCH;
-    if (cudaStreamWaitEvent(ss->s, ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    for (int c = 0; c <= cmax; ++c)
+      if (cudaStreamWaitEvent(ss->s[c], ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
   }
-  if (nbig_max > 0) k_scf<kScfBigThreads, 1><<<nbig_max, kScfBigThreads, 0, sb>>>(a, 1, nbig_max);
-  DXTB_CHECK_LAUNCH();
-  k_scf<kScfThreads, 2><<<nmol, kScfThreads, 0, st>>>(a, 0, nbig_max);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_scf<kScfThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  // largest classes first: clusters, then one-SM CTAs, then the shared SMs
+  for (int c = cmax; c >= 2; --c) {
+    const int csize = 1 << (c - 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(min(nmol, max(1, sms / csize)) * csize);
+    cfg.blockDim = dim3(kScfBigThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ss ? ss->s[c] : st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_scf_cluster, a, c) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  }
+  if (cmax >= 1) {
+    k_scf<kScfBigThreads, 1><<<nmol, kScfBigThreads, smem, ss ? ss->s[1] : st>>>(a, 1);
+    DXTB_CHECK_LAUNCH();
+  }
+  const size_t smem0 = (size_t)min(nmax, a.thr[1]) * (3 * sizeof(double) + 2 * sizeof(float));
+  k_scf<kScfThreads, 2><<<nmol, kScfThreads, smem0, ss ? ss->s[0] : st>>>(a, 0);
   DXTB_CHECK_LAUNCH();
   if (ss) {
-    if (cudaEventRecord(ss->join, ss->s) != cudaSuccess) return DXTB_ERR_LAUNCH;
-    if (cudaStreamWaitEvent(st, ss->join, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    for (int c = 0; c <= cmax; ++c) {
+      if (cudaEventRecord(ss->join[c], ss->s[c]) != cudaSuccess) return DXTB_ERR_LAUNCH;
+      if (cudaStreamWaitEvent(st, ss->join[c], 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    }
   }
   return DXTB_OK;
 }
 
 }  // namespace dxtb
+
+extern "C" int32_t dxtb_scf_set_size_classes(const int32_t *min_n) {
+  if (!min_n) return DXTB_ERR_ARGS;
+  for (int c = 1; c < kClasses; ++c)
+    if (min_n[c - 1] < 1 || (c > 1 && min_n[c - 1] < min_n[c - 2])) return DXTB_ERR_ARGS;
+  std::lock_guard<std::mutex> lock(g_policy_mutex);
+  for (int c = 1; c < kClasses; ++c) g_thr[c] = min_n[c - 1];
+  return DXTB_OK;
+}
 
 extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                             const double *overlap, const double *h0, const double *dipole,

@@ -213,7 +213,8 @@ int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
  * [naos] orbital charges, dp [natoms][3], qp [natoms][6] atomic multipoles,
  * vorb [naos], vdp [natoms][3], vqp [natoms][6] potentials of the final
  * charges, energies [nmol][4] = (E_h0 + E_interaction, -TS, iterations,
- * final residual) and status [nmol]. */
+ * final residual) and status [nmol]. Molecules run by size class (see
+ * dxtb_scf_set_size_classes); order lists them by non-increasing n. */
 int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                  const double *overlap, const double *h0, const double *dipole,
                  const double *quadrupole, const double *gamma,
@@ -225,6 +226,15 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                  double *coeff, double *evals, double *occ, double *q,
                  double *dp, double *qp, double *vorb, double *vdp,
                  double *vqp, double *energies, int32_t *status, void *stream);
+
+/* Size classes of the SCF launch (process-wide): molecules with n orbitals
+ * run, by class, one 256-thread CTA each two per SM (class 0), one
+ * 512-thread CTA on its own SM (class 1), or a thread-block cluster of 2, 4,
+ * 8 or 16 CTAs on as many SMs (classes 2-5) that share every O(n^3) phase.
+ * min_n[c-1] is the smallest n of class c (non-decreasing); the default is
+ * {128, 144, 192, 320, 640}. Clusters need the launch order of dxtb_scf;
+ * cluster sizes the GPU cannot place fold into the largest one it can. */
+int32_t dxtb_scf_set_size_classes(const int32_t *min_n);
 
 /* Nuclear gradient dE/dR [natoms][3] at the converged SCF (analytic
  * adjoint; the reference differentiates with autograd through
