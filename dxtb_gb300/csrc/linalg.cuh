@@ -234,82 +234,151 @@ __device__ void team_trinv(Team<CL> &tm, int n, const double *L, double *X) {
 // (lower variant): A = Q T Q^T. On exit d, e hold the diagonal and
 // sub-diagonal (e[i] couples i and i+1), the reflector of step k is stored
 // in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k]; d, e, tau
-// are written by the lead CTA. At step k every CTA holds the Householder
-// vector v and p = t A22 v - K v in shared memory (sv, sp: n doubles each),
-// and owns one contiguous chunk of the trailing rows: it forms those entries
-// of A22 v and applies the rank-2 update to those rows. pg: global [n]
-// exchange buffer for p. spart: shared [kPart].
+// are written by the lead CTA. Every CTA holds the column u of step k, then
+// the Householder vector v and p = t A22 v - K v in shared memory (su, sv,
+// sp: n doubles each), and owns one contiguous chunk of the trailing rows:
+// it forms those entries of A22 v and applies the rank-2 update to those
+// rows. The scalars of a step (column norm, beta, t, K) are formed by warp 0
+// alone from warp partials (fixed order) and broadcast through shared
+// memory: on this part every float64 operation repeated by all threads
+// costs FP64 pipe time. A one-CTA team captures the next column during the
+// update instead of reloading it. pg: global [n] exchange buffer for p
+// (clusters). spart: shared [kPart].
 template <bool CL>
 __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *e, double *tau,
-                             double *pg, double *sv, double *sp, double *spart, double *red) {
+                             double *pg, double *su, double *sv, double *sp, double *spart) {
+  __shared__ double swarp[32], swarp2[32], sscal[4];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
+  bool have_col = false;  // one-CTA team: su and swarp already hold this step's column
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
-    const double *col = A + (size_t)(k + 1) * n + k;  // col[r*n], r < m
-    double part = 0.0;
-    for (int r = threadIdx.x; r < m; r += blockDim.x) {
-      const double x = ld<CL>(col + (size_t)r * n);
-      sv[r] = x;
-      if (r > 0) part += x * x;
+    if (CL || !have_col) {
+      // the column below the diagonal and the warp partials of its norm
+      double part = 0.0;
+      for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        const double x = ld<CL>(A + (size_t)(k + 1 + r) * n + k);
+        su[r] = x;
+        if (r > 0) part = fma(x, x, part);
+      }
+      part = warp_sum(part);
+      if (tx == 0) swarp[ty] = part;
+      __syncthreads();
     }
-    const double sigma = block_sum(part, red);  // also orders the sv writes
-    const double alpha = ld<CL>(col);
-    double t = 0.0, beta = alpha;
-    if (sigma > 0.0) {
-      const double nrm = sqrt(alpha * alpha + sigma);
-      beta = alpha >= 0.0 ? -nrm : nrm;
-      t = (beta - alpha) / beta;
-      const double scale = 1.0 / (alpha - beta);
-      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) sv[r] *= scale;
-    }
-    if (threadIdx.x == 0) sv[0] = 1.0;
-    if (tm.lead() && threadIdx.x == 0) {
-      tau[k] = t;
-      e[k] = beta;
-      d[k] = ld<CL>(A + (size_t)k * n + k);
+    if (ty == 0) {
+      double sg = tx < nty ? swarp[tx] : 0.0;
+      sg = warp_sum(sg);  // butterfly order: the same value on every CTA
+      if (tx == 0) {
+        const double alpha = su[0];
+        double t = 0.0, beta = alpha, scale = 0.0, u0 = 0.0;
+        if (sg > 0.0) {
+          const double nrm = sqrt(alpha * alpha + sg);
+          beta = alpha >= 0.0 ? -nrm : nrm;
+          t = (beta - alpha) / beta;
+          u0 = alpha - beta;  // v = scale * (u0, u_1, u_2, ...)
+          scale = 1.0 / u0;
+        }
+        sscal[0] = t;
+        sscal[1] = scale;
+        sscal[2] = u0;
+        if (tm.lead()) {
+          tau[k] = t;
+          e[k] = beta;
+          d[k] = ld<CL>(A + (size_t)k * n + k);
+        }
+      }
     }
     __syncthreads();
+    const double t = sscal[0], scale = sscal[1], u0 = sscal[2];
+    have_col = false;
     if (t != 0.0) {  // the same on every CTA of the team
       const int r0 = (int)((int64_t)m * tm.rank / tm.size);
       const int r1 = (int)((int64_t)m * (tm.rank + 1) / tm.size);
       const int mc = r1 - r0;
       double *A22 = A + (size_t)(k + 1) * n + (k + 1);
       double *pdst = CL ? pg : sp;
+      const double ts = t * scale;
       // p_r = t (A22 v)_r for the own rows; A22 is symmetric, so row r of the
       // product reads column r (coalesced over r); the c range is split in G
       // groups so that all threads work
       const int G = (mc > 0 && mc < (int)blockDim.x) ? max(1, min(kPart / mc, (int)blockDim.x / mc)) : 1;
+      double kpart = 0.0;  // p . v over the own rows
       for (int q = threadIdx.x; q < G * mc; q += blockDim.x) {
         const int rr = q % mc, g = q / mc, r = r0 + rr;
-        double s = 0.0;
-        for (int c = g; c < m; c += G) s = fma(ld<CL>(A22 + (size_t)c * n + r), sv[c], s);
-        if (G > 1) spart[g * mc + rr] = s; else pdst[r] = t * s;
+        double s = g == 0 ? ld<CL>(A22 + r) * u0 : 0.0;
+        for (int c = g == 0 ? G : g; c < m; c += G) s = fma(ld<CL>(A22 + (size_t)c * n + r), su[c], s);
+        if (G > 1) {
+          spart[g * mc + rr] = s;
+        } else {
+          const double pr = ts * s;
+          pdst[r] = pr;
+          kpart = fma(pr, r == 0 ? 1.0 : scale * su[r], kpart);
+        }
       }
       if (G > 1) {
         __syncthreads();
         for (int rr = threadIdx.x; rr < mc; rr += blockDim.x) {
           double s = 0.0;
           for (int g = 0; g < G; ++g) s += spart[g * mc + rr];
-          pdst[r0 + rr] = t * s;
+          const int r = r0 + rr;
+          const double pr = ts * s;
+          pdst[r] = pr;
+          kpart = fma(pr, r == 0 ? 1.0 : scale * su[r], kpart);
         }
       }
-      tm.sync();  // p complete over the team
-      double part2 = 0.0;
-      for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        const double pr = CL ? __ldcg(pg + r) : sp[r];
-        if (CL) sp[r] = pr;
-        part2 += pr * sv[r];
-      }
-      const double K = 0.5 * t * block_sum(part2, red);
-      for (int r = threadIdx.x; r < m; r += blockDim.x) sp[r] -= K * sv[r];
-      // keep v (own rows) in column k for the back-transformation
-      for (int r = max(r0, 1) + threadIdx.x; r < r1; r += blockDim.x) A[(size_t)(k + 1 + r) * n + k] = sv[r];
+      kpart = warp_sum(kpart);
+      if (tx == 0) swarp2[ty] = kpart;
       __syncthreads();
-      // rank-2 update of the own rows, columns over lanes (coalesced)
+      if (ty == 0) {
+        double kk = tx < nty ? swarp2[tx] : 0.0;
+        kk = warp_sum(kk);
+        if (tx == 0) {
+          if constexpr (CL) {
+            double *slot = tm.gred + 16 * (tm.phase & 1);
+            slot[tm.rank] = kk;
+          } else {
+            sscal[3] = 0.5 * t * kk;
+          }
+        }
+      }
+      if constexpr (CL) {
+        double *slot = tm.gred + 16 * (tm.phase & 1);
+        ++tm.phase;
+        tm.sync();  // p and the CTA partials of p.v complete over the team
+        if (threadIdx.x == 0) {
+          double kk = 0.0;
+          for (int c = 0; c < tm.size; ++c) kk += __ldcg(slot + c);
+          sscal[3] = 0.5 * t * kk;
+        }
+      }
+      __syncthreads();
+      const double K = sscal[3];
+      // v and p - K v for all columns; v (own rows) kept in column k
+      for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        const double vc = c == 0 ? 1.0 : scale * su[c];
+        sv[c] = vc;
+        const double pc = CL ? __ldcg(pg + c) : sp[c];
+        sp[c] = fma(-K, vc, pc);
+        if (c >= r0 && c < r1 && c > 0) A[(size_t)(k + 1 + c) * n + k] = vc;
+      }
+      __syncthreads();
+      // rank-2 update of the own rows, columns over lanes (coalesced); a
+      // one-CTA team keeps the updated column 0 (rows >= 1) as the next column
+      double cpart = 0.0;
       for (int r = r0 + ty; r < r1; r += nty) {
         const double vr = sv[r], pr = sp[r];
         double *Wr = A22 + (size_t)r * n;
-        for (int c = tx; c < m; c += 32) Wr[c] = fma(-vr, sp[c], fma(-pr, sv[c], ld<CL>(Wr + c)));
+        for (int c = tx; c < m; c += 32) {
+          const double nw = fma(-vr, sp[c], fma(-pr, sv[c], ld<CL>(Wr + c)));
+          Wr[c] = nw;
+          if (!CL && c == 0 && r >= 1) {
+            su[r - 1] = nw;
+            if (r >= 2) cpart = fma(nw, nw, cpart);
+          }
+        }
+      }
+      if (!CL) {
+        if (tx == 0) swarp[ty] = cpart;
+        have_col = true;
       }
     }
     tm.sync();  // the next column is complete
@@ -649,41 +718,113 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
 
 // Y <- Q Y for the reflectors stored by team_tridiag (Q = H_0 ... H_{n-3});
 // Y is n x m row-major. Each CTA transforms its own block of columns, so no
-// team barrier is needed per reflector. w: global scratch of m doubles.
+// team barrier is needed. The reflectors are applied kNB at a time in the
+// compact WY form H_k0 ... H_k1-1 = I - V T V^T (T upper triangular, built as
+// in LAPACK dlarft, forward / columnwise): W = V^T Y, W <- T W,
+// Y <- Y - V W, about five CTA barriers per block instead of two or three
+// per reflector. wsc: global scratch of kNB * m doubles (each CTA uses its
+// own columns); spart: shared [kPart].
+constexpr int kNB = 16;
+
 template <bool CL>
 __device__ void team_back_transform(Team<CL> &tm, int n, const double *A, const double *tau, double *Y,
-                                    int m, double *w, double *spart) {
+                                    int m, double *wsc, double *spart) {
+  __shared__ double sT[kNB][kNB + 1];
+  __shared__ double sS[kNB][kNB + 1];
+  __shared__ double stau[kNB];
   const int j0 = (int)((int64_t)m * tm.rank / tm.size), j1 = (int)((int64_t)m * (tm.rank + 1) / tm.size);
   const int mc = j1 - j0;
-  if (mc > 0) {
-    for (int k = n - 3; k >= 0; --k) {
-      const double t = ld<CL>(tau + k);
-      if (t == 0.0) continue;
-      const int mm = n - k - 1;
-      const double *col = A + (size_t)(k + 1) * n + k;
-      double *Yb = Y + (size_t)(k + 1) * m + j0;
-      // w_j = t * v . Y[:, j]; the r range split into G groups (all threads busy)
-      const int G = mc < (int)blockDim.x ? max(1, min(kPart / mc, (int)blockDim.x / mc)) : 1;
-      for (int q = threadIdx.x; q < G * mc; q += blockDim.x) {
-        const int j = q % mc, g = q / mc;
-        double s = 0.0;
-        for (int r = g; r < mm; r += G)
-          s = fma(r == 0 ? 1.0 : ld<CL>(col + (size_t)r * n), ld<CL>(Yb + (size_t)r * m + j), s);
-        if (G > 1) spart[g * mc + j] = s; else w[j0 + j] = t * s;
-      }
-      __syncthreads();
-      if (G > 1) {
-        for (int j = threadIdx.x; j < mc; j += blockDim.x) {
-          double s = 0.0;
-          for (int g = 0; g < G; ++g) s += spart[g * mc + j];
-          w[j0 + j] = t * s;
+  const int nref = n - 2;  // reflectors 0 .. n-3 (the last ones may be identities)
+  double *W = wsc + (size_t)kNB * j0;  // kNB x mc, leading dimension mc
+  if (mc > 0 && nref > 0) {
+    for (int kb = ((nref - 1) / kNB) * kNB; kb >= 0; kb -= kNB) {
+      const int nb = min(kNB, nref - kb);
+      const int r0 = kb + 1, L = n - r0;  // rows touched by the block
+      // V(rho, i): reflector kb+i at local row rho = r - r0 (implicit 1 at rho = i)
+      auto vv = [&](int rho, int i) -> double {
+        return rho < i ? 0.0 : (rho == i ? 1.0 : ld<CL>(A + (size_t)(r0 + rho) * n + kb + i));
+      };
+      // (a) S = V^T V (strictly upper part) for T, rows split in G groups
+      const int npair = nb * (nb - 1) / 2;
+      if (threadIdx.x < nb) stau[threadIdx.x] = ld<CL>(tau + kb + threadIdx.x);
+      if (npair > 0) {
+        const int G = max(1, min(kPart / npair, (int)blockDim.x / npair));
+        for (int q = threadIdx.x; q < G * npair; q += blockDim.x) {
+          const int pr = q % npair, g = q / npair;
+          int j = (int)((sqrt(8.0 * (double)pr + 1.0) + 1.0) * 0.5);  // pr -> (i < j)
+          while (j * (j - 1) / 2 > pr) --j;
+          while ((j + 1) * j / 2 <= pr) ++j;
+          const int i = pr - j * (j - 1) / 2;
+          double acc = 0.0;
+          for (int rho = j + g; rho < L; rho += G) acc = fma(vv(rho, i), vv(rho, j), acc);
+          spart[g * npair + pr] = acc;
         }
         __syncthreads();
+        for (int pr = threadIdx.x; pr < npair; pr += blockDim.x) {
+          int j = (int)((sqrt(8.0 * (double)pr + 1.0) + 1.0) * 0.5);
+          while (j * (j - 1) / 2 > pr) --j;
+          while ((j + 1) * j / 2 <= pr) ++j;
+          const int i = pr - j * (j - 1) / 2;
+          double acc = 0.0;
+          for (int g = 0; g < G; ++g) acc += spart[g * npair + pr];
+          sS[i][j] = acc;
+        }
       }
-      for (int64_t q = threadIdx.x; q < (int64_t)mm * mc; q += blockDim.x) {
-        const int r = (int)(q / mc), j = (int)(q % mc);
-        const double vr = r == 0 ? 1.0 : ld<CL>(col + (size_t)r * n);
-        Yb[(size_t)r * m + j] = ld<CL>(Yb + (size_t)r * m + j) - vr * w[j0 + j];
+      __syncthreads();
+      // (b) T: lane i builds row i, T[i][j] = -tau_j sum_{l=i}^{j-1} T[i][l] S[l][j]
+      if (threadIdx.x < nb) {
+        const int i = threadIdx.x;
+        for (int j = 0; j < nb; ++j) {
+          if (j < i) {
+            sT[i][j] = 0.0;
+          } else if (j == i) {
+            sT[i][j] = stau[i];
+          } else {
+            double acc = 0.0;
+            for (int l = i; l < j; ++l) acc = fma(sT[i][l], sS[l][j], acc);
+            sT[i][j] = -stau[j] * acc;
+          }
+        }
+      }
+      // (c) W = V^T Y (nb x mc), rows split in G groups
+      {
+        const int nout = nb * mc;
+        const int G = nout < (int)blockDim.x ? max(1, min(kPart / nout, (int)blockDim.x / nout)) : 1;
+        for (int q = threadIdx.x; q < G * nout; q += blockDim.x) {
+          const int o = q % nout, g = q / nout;
+          const int i = o / mc, j = o % mc;
+          double acc = 0.0;
+          for (int rho = i + g; rho < L; rho += G)
+            acc = fma(vv(rho, i), ld<CL>(Y + (size_t)(r0 + rho) * m + j0 + j), acc);
+          if (G > 1) spart[g * nout + o] = acc; else W[(size_t)i * mc + j] = acc;
+        }
+        __syncthreads();
+        if (G > 1) {
+          for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+            double acc = 0.0;
+            for (int g = 0; g < G; ++g) acc += spart[g * nout + o];
+            W[(size_t)(o / mc) * mc + o % mc] = acc;
+          }
+          __syncthreads();
+        }
+      }
+      // (d) W <- T W, one column per thread, rows ascending in place
+      for (int j = threadIdx.x; j < mc; j += blockDim.x) {
+        for (int i = 0; i < nb; ++i) {
+          double acc = 0.0;
+          for (int l = i; l < nb; ++l) acc = fma(sT[i][l], W[(size_t)l * mc + j], acc);
+          W[(size_t)i * mc + j] = acc;
+        }
+      }
+      __syncthreads();
+      // (e) Y <- Y - V W
+      for (int64_t q = threadIdx.x; q < (int64_t)L * mc; q += blockDim.x) {
+        const int rho = (int)(q / mc), j = (int)(q % mc);
+        double *y = Y + (size_t)(r0 + rho) * m + j0 + j;
+        double acc = ld<CL>(y);
+        const int imax = min(nb - 1, rho);
+        for (int i = 0; i <= imax; ++i) acc = fma(-vv(rho, i), W[(size_t)i * mc + j], acc);
+        *y = acc;
       }
       __syncthreads();
     }

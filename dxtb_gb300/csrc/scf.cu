@@ -34,11 +34,16 @@ struct MolView {
 };
 
 __host__ __device__ inline int64_t lu_slots(int64_t n) { return n < kLuSlots ? n : kLuSlots; }
+// inverse-iteration factors, reused afterwards by the blocked back-transform (16 n)
+__host__ __device__ inline int64_t lu_size(int64_t n) {
+  const int64_t a = 5 * n * lu_slots(n), b = 16 * n;
+  return a > b ? a : b;
+}
 
 // Per-molecule workspace layout (doubles).
 __host__ __device__ inline int64_t ws_size_mol(int64_t n, int64_t nat) {
   const int64_t N = n + 9 * nat;
-  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + 5 * n * lu_slots(n) + n + 8 +
+  return 3 * n * n + 10 * n + (2 * kRank + 7) * N + 64 + 16 * nat + lu_size(n) + n + 8 +
          4 * kRank + 64 + 64;
 }
 
@@ -72,7 +77,7 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.xold = q; q += N;
   w.rold = q; q += N;
   w.xbest = q; q += N;
-  w.lu = q; q += (size_t)5 * n * lu_slots(n);
+  w.lu = q; q += (size_t)lu_size(n);
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
   w.sdot = q; q += 4 * kRank + 64;
   w.team = q; q += 64;  // [0, 32) partial sums, [32, 48) broadcast words (int)
@@ -484,7 +489,7 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
     }
     tm.sync();
     // ---- eigenvalues: Householder tridiagonalisation + bisection/Newton ----
-    team_tridiag(tm, n, w.A, w.d, w.e, w.tau, w.p, sd, se, spart, red);
+    team_tridiag(tm, n, w.A, w.d, w.e, w.tau, w.p, sd, se, sw, spart);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       sd[i] = ld<CL>(w.d + i);
       se[i] = ld<CL>(w.e + i);
@@ -525,7 +530,7 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
     mo = ldi<CL>(tm.gctl + 1);
     // ---- eigenvectors of the mo lowest orbitals only ----
     team_tri_vectors(tm, n, sd, se, sw, mo, tnorm, w.Zt, w.lu, (int)min((int64_t)tm.nthr, lu_slots(n)), w.cl);
-    team_back_transform(tm, n, w.A, w.tau, w.Zt, mo, w.p, spart);
+    team_back_transform(tm, n, w.A, w.tau, w.Zt, mo, w.lu, spart);  // lu: free after the vectors
     // ---- C^T = Y^T X (orbital j is row j; X lower -> k >= i) ----
     team_gemm<true, false>(tm, mo, n, n, 1.0, w.Zt, mo, w.Linv, n, 0.0, C, n, kBUpper);
     // ---- density P = C diag(occ) C^T (scf/utils.py:29-52) ----
