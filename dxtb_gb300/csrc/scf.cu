@@ -690,7 +690,7 @@ namespace dxtb {
 
 // Size-class thresholds (smallest n of classes 1..5), process-wide.
 static std::mutex g_policy_mutex;
-static int g_thr[kClasses] = {0, 128, 144, 192, 320, 640};
+static int g_thr[kClasses] = {0, 112, 136, 160, 320, 640};
 
 // Side streams and fork/join events per (device, caller stream), created once
 // (no device memory is allocated); all launches stay inside a caller's

@@ -232,7 +232,7 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
  * 512-thread CTA on its own SM (class 1), or a thread-block cluster of 2, 4,
  * 8 or 16 CTAs on as many SMs (classes 2-5) that share every O(n^3) phase.
  * min_n[c-1] is the smallest n of class c (non-decreasing); the default is
- * {128, 144, 192, 320, 640}. Clusters need the launch order of dxtb_scf;
+ * {112, 136, 160, 320, 640}. Clusters need the launch order of dxtb_scf;
  * cluster sizes the GPU cannot place fold into the largest one it can. */
 int32_t dxtb_scf_set_size_classes(const int32_t *min_n);
 
