@@ -55,6 +55,7 @@ _SIGS = {
     "dxtb_index_sizes": (i32, [vp, i32, i32, i32, vp, vp, vp]),
     "dxtb_index_maps": (i32, [vp, i32, i32, i32, vp, vp, i64, i64] + [vp] * 14 + [vp]),
     "dxtb_scf_set_size_classes": (i32, [vp]),
+    "dxtb_scf_get_size_classes": (i32, [vp]),
     "dxtb_born_matrix": (i32, [vp, vp, vp, f64, i32, i32, f64, f64, vp, vp, vp, vp]),
     "dxtb_born_gradient": (i32, [vp, vp, vp, f64, i32, i32, f64, f64, vp, vp, vp, vp, vp]),
     "dxtb_fp64_fma_probe": (i32, [i64, i32, i32, vp, vp]),

@@ -550,6 +550,7 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
       }
     }
     double x = 0.5 * (l + h);
+    const double del = 8.0 * kEps * fmax(tnorm, 1.0);  // resolution of the counts
     if (cl == k && ch == k + 1) {
       // --- safeguarded Newton on p(x): one root in (l, h) ---
       x = fmin(fmax(x0, l), h);
@@ -570,6 +571,20 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
           if (sturm_count_f64(n, d, e2, x) <= k) l = x; else h = x;
           if (h - l <= tol) break;
         }
+      }
+      // the characteristic-polynomial recurrence loses accuracy for large n:
+      // accept x only if the (backward-stable) counts put the k-th
+      // eigenvalue within del of it, else bisect to that resolution
+      const int cxl = sturm_count_f64(n, d, e2, x - del);
+      const int cxh = sturm_count_f64(n, d, e2, x + del);
+      if (!(cxl <= k && k < cxh)) {
+        if (cxl > k) h = fmin(h, x - del); else l = fmax(l, x + del);
+        for (int it = 0; it < 200 && h - l > 2.0 * del; ++it) {
+          const double mid = 0.5 * (l + h);
+          if (mid <= l || mid >= h) break;
+          if (sturm_count_f64(n, d, e2, mid) <= k) l = mid; else h = mid;
+        }
+        x = 0.5 * (l + h);
       }
     }
     lam[k] = x;

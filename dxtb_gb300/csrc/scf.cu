@@ -854,6 +854,13 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
 
 }  // namespace dxtb
 
+extern "C" int32_t dxtb_scf_get_size_classes(int32_t *min_n) {
+  if (!min_n) return DXTB_ERR_ARGS;
+  std::lock_guard<std::mutex> lock(g_policy_mutex);
+  for (int c = 1; c < kClasses; ++c) min_n[c - 1] = g_thr[c];
+  return DXTB_OK;
+}
+
 extern "C" int32_t dxtb_scf_set_size_classes(const int32_t *min_n) {
   if (!min_n) return DXTB_ERR_ARGS;
   for (int c = 1; c < kClasses; ++c)

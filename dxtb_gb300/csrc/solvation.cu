@@ -233,11 +233,14 @@ __global__ void k_born_grad(dxtb_batch b, const double *__restrict__ pf_, GbPar 
         r = sqrt(dx * dx + dy * dy + dz * dz);
       }
       gb_kernel(p.kernel, r, sb[k] * sb[j], &fr, &fa);
-      s += qa[j] * fa * sb[j];
+      // an infinite Born radius (saturated OBC tanh, buried atoms of dense
+      // systems) decouples the pair: f and its derivatives vanish faster than
+      // B grows, so the limit of the term is 0 (the product would be 0 * inf)
+      if (isfinite(sb[j]) && isfinite(sb[k])) s += qa[j] * fa * sb[j];
     }
     double dbdpsi;
     born_of_psi(psi[a0 + k], rv[k], p, &dbdpsi);
-    dpsi[k] = p.keps * qa[k] * s * dbdpsi;
+    dpsi[k] = isfinite(dbdpsi) && isfinite(sb[k]) ? p.keps * qa[k] * s * dbdpsi : 0.0;
   }
   __syncthreads();
   // ALPB shape term 1/2 keps alpbet adet (sum q)^2 (zero for neutral molecules)
@@ -259,7 +262,7 @@ __global__ void k_born_grad(dxtb_batch b, const double *__restrict__ pf_, GbPar 
       const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
       double fr, fa;
       gb_kernel(p.kernel, r, sb[i] * sb[j], &fr, &fa);
-      double G = p.keps * qa[i] * qa[j] * fr;
+      double G = isfinite(fr) ? p.keps * qa[i] * qa[j] * fr : 0.0;
       if (r <= kBornCutoff) {
         double h, dh;
         psi_term(r, rhoi, rv[j], h, dh);  // i descreens j

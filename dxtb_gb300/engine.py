@@ -182,6 +182,16 @@ def _seg_sum(values: torch.Tensor, seg: torch.Tensor, nmol: int) -> torch.Tensor
 GB_KERNELS = {"p16": 0, "still": 1}
 
 
+def scf_launches(L, nmax: int) -> int:
+    """Kernels launched by dxtb_scf for a batch whose largest molecule has
+    nmax orbitals: one per cluster class up to the largest one present, the
+    one-SM launch, the shared-SM launch."""
+    thr = (C.c_int32 * 5)()
+    _lib.check(L.dxtb_scf_get_size_classes(thr), "size classes")
+    cmax = sum(1 for t in thr if nmax >= t)
+    return 1 + (1 if cmax >= 1 else 0) + max(0, cmax - 1)
+
+
 def gb_args(gb: dict) -> tuple:
     """
     (epsilon, kernel, alpb, born_scale, born_offset) of a solvation dict with
@@ -301,7 +311,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                    en.data_ptr(), status.data_ptr(), st),
         "SCF",
     )
-    launches += 2  # large- and small-molecule SCF kernels
+    launches += scf_launches(L, int(pb.nao.max()))
     mark("scf", 1)
     e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
     e_rep = _seg_sum(erep[:na], pb.t["atom_mol"], pb.nmol)

@@ -92,37 +92,73 @@ class Server:
     forces, iterations, status)``. Packs are admitted FIFO: the oldest
     queued request fixes the pack's method, and younger requests of that
     method join while they fit.
+
+    With ``large_slots`` > 0, requests of at least ``large_n`` orbitals
+    (``executor.norb(req)``) form a second lane: they queue apart, use the
+    last ``large_slots`` slots and go out in packs of at most
+    ``large_pack``. A pack returns when its slowest member is done, so small
+    requests would otherwise wait for the largest molecule admitted with
+    them. Small requests may use an idle large slot while no large request
+    is queued.
     """
 
+    LANES = ("large", "small")
+
     def __init__(self, executor, *, hbm_budget: float = 120e9, slots: int = 8, max_pack: int = 32,
+                 large_slots: int = 0, large_n: int | None = None, large_pack: int = 4,
                  clock=time.perf_counter):
-        if slots < 1 or max_pack < 1:
-            raise ValueError("slots and max_pack must be positive")
+        if slots < 1 or max_pack < 1 or large_pack < 1:
+            raise ValueError("slots and pack sizes must be positive")
+        if not 0 <= large_slots < slots:
+            raise ValueError("large_slots must leave at least one small slot")
+        if large_slots > 0 and large_n is None:
+            raise ValueError("a large lane needs large_n")
         self.ex = executor
         self.budget = int(hbm_budget)
         self.slots = slots
         self.max_pack = max_pack
+        self.large_slots = large_slots
+        self.large_n = large_n
+        self.large_pack = large_pack
         self.clock = clock
         self.t0 = clock()
-        self.queue: deque = deque()
-        self.free_slots = list(range(slots))
+        self.queues = {"small": deque(), "large": deque()}
+        self.free = {"small": list(range(slots - large_slots)),
+                     "large": list(range(slots - large_slots, slots))}
         self.inflight: list[_Pack] = []
         self.used = 0
         self.stats = Stats()
         self._pid = 0
 
+    @property
+    def queue(self) -> list:
+        """Queued requests (large lane first)."""
+        return list(self.queues["large"]) + list(self.queues["small"])
+
+    @property
+    def free_slots(self) -> list:
+        return self.free["small"] + self.free["large"]
+
     def now(self) -> float:
         return self.clock() - self.t0
+
+    def lane(self, req: Request) -> str:
+        if self.large_slots > 0 and self.ex.norb(req) >= self.large_n:
+            return "large"
+        return "small"
 
     def submit(self, req: Request) -> None:
         if req.method not in METHODS:
             raise ValueError(f"unknown method {req.method!r}")
-        self.queue.append(req)
+        self.queues[self.lane(req)].append(req)
         self.stats.requests += 1
 
     @property
     def idle(self) -> bool:
-        return not self.queue and not self.inflight
+        return not self.queues["small"] and not self.queues["large"] and not self.inflight
+
+    def _slot_lane(self, slot: int) -> str:
+        return "large" if slot >= self.slots - self.large_slots else "small"
 
     def _reap(self) -> list[Response]:
         out = []
@@ -137,48 +173,67 @@ class Server:
                 out.append(Response(r.rid, float(e), f, int(it), int(st), r.arrival, pk.admitted, t,
                                     pk.pid, len(pk.requests)))
             self.used -= pk.nbytes
-            self.free_slots.append(pk.slot)
+            self.free[self._slot_lane(pk.slot)].append(pk.slot)
             pk.handle = None
         self.inflight = keep
         return out
 
+    def _take_slot(self, lane: str) -> int | None:
+        if self.free[lane]:
+            return self.free[lane].pop(0)
+        if lane == "small" and not self.queues["large"] and self.free["large"]:
+            return self.free["large"].pop(0)
+        return None
+
     def _admit(self) -> list[Response]:
         out = []
-        while self.free_slots and self.queue:
-            head = self.queue[0]
-            free = self.budget - self.used
-            nb = self.ex.nbytes(head)
-            if nb > self.budget:
-                # can never fit: answer it with an error instead of blocking the queue
-                self.queue.popleft()
-                t = self.now()
-                out.append(Response(head.rid, math.nan, None, 0, 7, head.arrival, t, t, -1, 0,
-                                    error="request exceeds the HBM budget"))
-                self.stats.rejected += 1
-                continue
-            if nb > free:
-                break  # wait for memory: in-flight packs will release it
-            take, rest, tot = [], deque(), 0
-            while self.queue:
-                r = self.queue.popleft()
-                if len(take) < self.max_pack and r.method == head.method:
-                    b = nb if r is head else self.ex.nbytes(r)
-                    if tot + b <= free:
-                        take.append(r)
-                        tot += b
-                        continue
-                rest.append(r)
-            self.queue = rest
-            slot = self.free_slots.pop(0)
-            pk = _Pack(self._pid, slot, take, tot, self.now())
-            self._pid += 1
-            pk.handle = self.ex.launch(take, slot)
-            self.inflight.append(pk)
-            self.used += tot
-            self.stats.packs += 1
-            self.stats.pack_sizes.append(len(take))
-            self.stats.max_inflight = max(self.stats.max_inflight, len(self.inflight))
-            self.stats.max_bytes = max(self.stats.max_bytes, self.used)
+        progressed = True
+        while progressed:
+            progressed = False
+            for lane in self.LANES:
+                q = self.queues[lane]
+                if not q:
+                    continue
+                if not self.free[lane] and not (lane == "small" and not self.queues["large"]
+                                                and self.free["large"]):
+                    continue
+                head = q[0]
+                free = self.budget - self.used
+                nb = self.ex.nbytes(head)
+                if nb > self.budget:
+                    # can never fit: answer it with an error instead of blocking the queue
+                    q.popleft()
+                    t = self.now()
+                    out.append(Response(head.rid, math.nan, None, 0, 7, head.arrival, t, t, -1, 0,
+                                        error="request exceeds the HBM budget"))
+                    self.stats.rejected += 1
+                    progressed = True
+                    continue
+                if nb > free:
+                    continue  # wait for memory: in-flight packs will release it
+                cap = self.large_pack if lane == "large" else self.max_pack
+                take, rest, tot = [], deque(), 0
+                while q:
+                    r = q.popleft()
+                    if len(take) < cap and r.method == head.method:
+                        b = nb if r is head else self.ex.nbytes(r)
+                        if tot + b <= free:
+                            take.append(r)
+                            tot += b
+                            continue
+                    rest.append(r)
+                self.queues[lane] = rest
+                slot = self._take_slot(lane)
+                pk = _Pack(self._pid, slot, take, tot, self.now())
+                self._pid += 1
+                pk.handle = self.ex.launch(take, slot)
+                self.inflight.append(pk)
+                self.used += tot
+                self.stats.packs += 1
+                self.stats.pack_sizes.append(len(take))
+                self.stats.max_inflight = max(self.stats.max_inflight, len(self.inflight))
+                self.stats.max_bytes = max(self.stats.max_bytes, self.used)
+                progressed = True
         return out
 
     def pump(self) -> list[Response]:
@@ -280,6 +335,10 @@ class CudaExecutor:
         tb.check_elements(z)
         return int(tb.el_nao[z].sum()), len(z), int(tb.el_nsh[z].sum())
 
+    def norb(self, req: Request) -> int:
+        """Orbitals of the request's molecule."""
+        return self._sizes(req)[0]
+
     def nbytes(self, req: Request) -> int:
         """Device bytes of one request's state (integrals, caches, SCF workspace, outputs)."""
         from . import _lib
@@ -371,17 +430,22 @@ def main(argv=None) -> None:
     p.add_argument("--slots", type=int, default=8)
     p.add_argument("--max-pack", type=int, default=32)
     p.add_argument("--budget-gb", type=float, default=120.0)
+    p.add_argument("--large-slots", type=int, default=3, help="slots of the large-molecule lane (0: one lane)")
+    p.add_argument("--large-n", type=int, default=320, help="orbitals from which a request is large")
+    p.add_argument("--large-pack", type=int, default=4)
     a = p.parse_args(argv)
     methods = tuple(a.methods.split(","))
     reqs = poisson_requests(a.requests, a.rate, a.seed, methods=methods, nat_range=tuple(a.nat))
     ex = CudaExecutor(slots=a.slots)
     warm_up(ex, a.slots)
-    srv = Server(ex, hbm_budget=a.budget_gb * 1e9, slots=a.slots, max_pack=a.max_pack)
+    srv = Server(ex, hbm_budget=a.budget_gb * 1e9, slots=a.slots, max_pack=a.max_pack,
+                 large_slots=a.large_slots, large_n=a.large_n, large_pack=a.large_pack)
     out = srv.serve(reqs)
     s = latency_summary(out)
     s.update({
         "rate_hz": a.rate, "nat_range": list(a.nat), "methods": list(methods), "seed": a.seed,
         "slots": a.slots, "max_pack": a.max_pack, "budget_gb": a.budget_gb,
+        "large_slots": a.large_slots, "large_n": a.large_n, "large_pack": a.large_pack,
         "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
         "max_bytes_gb": srv.stats.max_bytes / 1e9,
         "iterations_max": max(r.iterations for r in out),

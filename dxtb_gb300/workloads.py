@@ -25,31 +25,39 @@ def _unit(rng) -> np.ndarray:
 
 
 def build_geometry(rng, heavy: list[int], nh: int) -> tuple[np.ndarray, np.ndarray]:
-    pos: list[np.ndarray] = []
-    for k, _ in enumerate(heavy):
-        if k == 0:
-            pos.append(np.zeros(3))
+    """Place the heavy atoms by the random walk, then the hydrogens; the
+    distance test against all placed atoms is one vectorised pass."""
+    arr = np.empty((len(heavy) + nh, 3))
+    k = 0
+    for i, _ in enumerate(heavy):
+        if i == 0:
+            arr[0] = 0.0
+            k = 1
             continue
         for _try in range(100000):
-            anchor = pos[rng.integers(len(pos))]
+            anchor = arr[rng.integers(k)]
             p = anchor + rng.uniform(2.6, 2.9) * _unit(rng)
-            if min(np.linalg.norm(p - q) for q in pos) >= 2.0:
-                pos.append(p)
+            dd = p - arr[:k]
+            if np.sqrt(np.einsum("ij,ij->i", dd, dd)).min() >= 2.0:
+                arr[k] = p
+                k += 1
                 break
         else:
             raise RuntimeError("could not place heavy atom")
-    nheavy = len(pos)
+    nheavy = k
     for _ in range(nh):
         for _try in range(100000):
-            anchor = pos[rng.integers(nheavy)]
+            anchor = arr[rng.integers(nheavy)]
             p = anchor + 2.05 * _unit(rng)
-            if min(np.linalg.norm(p - q) for q in pos) >= 2.0:
-                pos.append(p)
+            dd = p - arr[:k]
+            if np.sqrt(np.einsum("ij,ij->i", dd, dd)).min() >= 2.0:
+                arr[k] = p
+                k += 1
                 break
         else:
             raise RuntimeError("could not place hydrogen")
     numbers = np.array(list(heavy) + [1] * nh, dtype=np.int64)
-    return numbers, np.array(pos)
+    return numbers, arr[:k].copy()
 
 
 def random_molecule(seed: int, nat: int) -> tuple[np.ndarray, np.ndarray]:

@@ -235,6 +235,8 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
  * {112, 136, 160, 320, 640}. Clusters need the launch order of dxtb_scf;
  * cluster sizes the GPU cannot place fold into the largest one it can. */
 int32_t dxtb_scf_set_size_classes(const int32_t *min_n);
+/* The current thresholds (min_n [5]). */
+int32_t dxtb_scf_get_size_classes(int32_t *min_n);
 
 /* Nuclear gradient dE/dR [natoms][3] at the converged SCF (analytic
  * adjoint; the reference differentiates with autograd through

@@ -42,6 +42,9 @@ class FakeExecutor:
     def collect(self, h):
         return [(-float(len(r.numbers)), None, 5, 0) for r in h["reqs"]]
 
+    def norb(self, r):
+        return 2 * len(r.numbers)
+
 
 def _req(rid, method="gfn2", nat=10, t=0.0):
     return Request(rid, method, np.ones(nat, dtype=np.int64), np.zeros((nat, 3)), arrival=t)
@@ -106,6 +109,40 @@ def test_slots_bound_inflight_packs():
     # FIFO: admission times are non-decreasing in request id
     adm = [r.admitted for r in sorted(done, key=lambda r: r.rid)]
     assert adm == sorted(adm)
+
+
+def test_large_lane_keeps_small_requests_moving():
+    clk = FakeClock()
+    ex = FakeExecutor(clk, cost=1e-3)
+    # orbitals = 2 nat; large lane from 200 orbitals (nat >= 100), 1 of 3 slots
+    srv = Server(ex, hbm_budget=1e12, slots=3, max_pack=8, large_slots=1, large_n=200, large_pack=2,
+                 clock=clk)
+    big = [_req(i, nat=300) for i in range(3)]          # 0.3 s each pack
+    small = [_req(10 + i, nat=10) for i in range(12)]  # 0.01 s each pack
+    for r in big + small:
+        srv.submit(r)
+    assert [r.rid for r in srv.queues["large"]] == [0, 1, 2]
+    srv.pump()
+    # the large slot takes at most large_pack big requests; small packs fill the rest
+    assert ex.launched[0][0] == [0, 1] and ex.launched[0][1] == 2
+    assert all(len(ids) <= 8 and min(ids) >= 10 for ids, _, _ in ex.launched[1:])
+    done = {}
+    while not srv.idle:
+        for x in srv.pump():
+            done[x.rid] = x.done
+        clk.t += 0.005
+    # every small request finishes before the second large pack does
+    assert max(done[10 + i] for i in range(12)) < done[2]
+
+
+def test_small_requests_borrow_idle_large_slots():
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    srv = Server(ex, hbm_budget=1e12, slots=2, max_pack=1, large_slots=1, large_n=200, clock=clk)
+    for i in range(3):
+        srv.submit(_req(i, nat=10))
+    srv.pump()
+    assert sorted(slot for _, slot, _ in ex.launched) == [0, 1]  # no large request queued
 
 
 def test_latency_summary_and_poisson_stream():
