@@ -319,10 +319,10 @@ def main():
         ex = CudaExecutor(dev, slots=a.serve_slots)
         warm_up(ex, a.serve_slots)
         torch.cuda.synchronize()
-        srv = Server(ex, hbm_budget=120e9, slots=a.serve_slots, max_pack=32)
+        srv = Server(ex, hbm_budget=120e9, slots=a.serve_slots, max_pack=32, order="size")
         out = srv.serve(reqs)
         serving = latency_summary(out)
-        serving.update({"rate_hz": a.serve_rate, "slots": a.serve_slots, "max_pack": 32,
+        serving.update({"rate_hz": a.serve_rate, "slots": a.serve_slots, "max_pack": 32, "order": "size",
                         "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
                         "hbm_budget_gb": 120.0, "status_bad": sum(1 for r in out if r.status != 0)})
 

@@ -26,6 +26,7 @@
 namespace dxtb {
 
 constexpr int kPart = 512;  // shared partial sums of the split dot products
+constexpr int kVerifyN = 384;  // eigenvalues are checked by Sturm counts above this order
 
 __device__ __forceinline__ unsigned cluster_ctarank() {
   unsigned r;
@@ -572,11 +573,12 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
           if (h - l <= tol) break;
         }
       }
-      // the characteristic-polynomial recurrence loses accuracy for large n:
-      // accept x only if the (backward-stable) counts put the k-th
-      // eigenvalue within del of it, else bisect to that resolution
-      const int cxl = sturm_count_f64(n, d, e2, x - del);
-      const int cxh = sturm_count_f64(n, d, e2, x + del);
+      // the characteristic-polynomial recurrence loses accuracy for large n
+      // (1e-10 |T| at n = 4748): there, accept x only if the
+      // (backward-stable) counts put the k-th eigenvalue within del of it,
+      // else bisect to that resolution
+      const int cxl = n > kVerifyN ? sturm_count_f64(n, d, e2, x - del) : k;
+      const int cxh = n > kVerifyN ? sturm_count_f64(n, d, e2, x + del) : k + 1;
       if (!(cxl <= k && k < cxh)) {
         if (cxl > k) h = fmin(h, x - del); else l = fmax(l, x + del);
         for (int it = 0; it < 200 && h - l > 2.0 * del; ++it) {
@@ -695,6 +697,7 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         // forward: apply the row interchanges and multipliers (the running
         // row stays in a register; the loads do not depend on the chain)
         double carry = Y[j];
+#pragma unroll 4
         for (int i = 0; i < n - 1; ++i) {
           double xi = carry, xn = Y[(size_t)(i + 1) * m + j];
           if (LU(Pv, i) != 0.0) {
@@ -708,6 +711,7 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         Y[(size_t)(n - 1) * m + j] = carry;
         // back substitution with the upper factor (two super-diagonals)
         double x1 = 0.0, x2 = 0.0;
+#pragma unroll 4
         for (int i = n - 1; i >= 0; --i) {
           const double v = (Y[(size_t)i * m + j] - LU(U1, i) * x1 - LU(U2, i) * x2) * LU(U0, i);
           Y[(size_t)i * m + j] = v;

@@ -459,25 +459,39 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
   while (status == DXTB_OK) {
     ++it;
     // ---- Fock matrix F(x) into Zt (conversions.py:255-297) ----
-    for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
-      const int i = (int)(t / n), j = (int)(t % n);
-      double f = H0[t] - 0.5 * S[t] * (ld<CL>(w.x + i) + ld<CL>(w.x + j));
-      if (multipole) {
-        const int ai = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + i]];
-        const int aj = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + j]];
-        const int64_t e1 = mv.moff + t, e2 = mv.moff + (int64_t)j * n + i;
-        double acc = 0.0;
-        for (int c = 0; c < 3; ++c)
-          acc += a.D[c * mv.mtot + e1] * ld<CL>(w.x + n + 3 * aj + c) +
-                 a.D[c * mv.mtot + e2] * ld<CL>(w.x + n + 3 * ai + c);
-        for (int c = 0; c < 6; ++c)
-          acc += a.Q[c * mv.mtot + e1] * ld<CL>(w.x + n + 3 * nat + 6 * aj + c) +
-                 a.Q[c * mv.mtot + e2] * ld<CL>(w.x + n + 3 * nat + 6 * ai + c);
-        f -= 0.5 * acc;
+    // The multipole part -1/2 (T + T^T) with T_ij = sum_c M_c,ij v_c(atom of j)
+    // is formed in two coalesced passes (T into A, then the transposed read),
+    // the orbital -> atom map and the orbital potential staged in shared
+    // memory (free here: df and sd are used later in the iteration).
+    {
+      int *aoat = reinterpret_cast<int *>(df);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        aoat[i] = b.shell_atom[mv.s0 + b.ao_shell[mv.o0 + i]];
+        sd[i] = ld<CL>(w.x + i);
       }
-      w.Zt[t] = f;
+      __syncthreads();
+      if (multipole) {
+        const double *xd = w.x + n, *xq = w.x + n + 3 * nat;
+        const double *Dm = a.D + mv.moff, *Qm = a.Q + mv.moff;
+        for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
+          const int aj = aoat[(int)(t % n)];
+          double acc = 0.0;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc = fma(Dm[c * mv.mtot + t], ld<CL>(xd + 3 * aj + c), acc);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) acc = fma(Qm[c * mv.mtot + t], ld<CL>(xq + 6 * aj + c), acc);
+          w.A[t] = acc;
+        }
+        tm.sync();
+      }
+      for (int64_t t = tm.tid; t < (int64_t)n * n; t += tm.nthr) {
+        const int i = (int)(t / n), j = (int)(t % n);
+        double f = H0[t] - 0.5 * S[t] * (sd[i] + sd[j]);
+        if (multipole) f -= 0.5 * (ld<CL>(w.A + t) + ld<CL>(w.A + (size_t)j * n + i));
+        w.Zt[t] = f;
+      }
+      tm.sync();
     }
-    tm.sync();
     // ---- F' = X F X^T (exlibs/xitorch/_impls/linalg/symeig.py:57-61) ----
     // X = L^-1 is lower triangular: A = X F needs k <= i; only the lower
     // triangle of (X F) X^T is formed (k <= j), then mirrored.
@@ -723,12 +737,18 @@ static int32_t side_stream(cudaStream_t caller, SideStream **out) {
     if (!ss.used && slot == nullptr) slot = &ss;
   }
   if (slot == nullptr) return DXTB_OK;
-  // the larger classes run on the highest-priority streams: their CTAs need
-  // whole SMs and bound the batch's makespan, so they are dispatched first
-  int least = 0, greatest = 0;
+  // By default the larger classes run on the higher-priority streams: their
+  // CTAs need whole SMs and bound a batch's makespan, so they are dispatched
+  // first. A caller stream with a priority of its own (a serving loop that
+  // ranks its lanes) passes it on to every class instead.
+  int least = 0, greatest = 0, cprio = 0;
   if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return DXTB_ERR_LAUNCH;
+  if (caller == nullptr || cudaStreamGetPriority(caller, &cprio) != cudaSuccess) {
+    cudaGetLastError();
+    cprio = least;
+  }
   for (int c = 0; c < kClasses; ++c) {
-    const int prio = max(greatest, least - c);  // class 0: the lowest priority
+    const int prio = cprio != least ? cprio : max(greatest, least - c);  // class 0: the lowest
     if (cudaStreamCreateWithPriority(&slot->s[c], cudaStreamNonBlocking, prio) != cudaSuccess)
       return DXTB_ERR_LAUNCH;
     if (cudaEventCreateWithFlags(&slot->join[c], cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;

@@ -99,14 +99,17 @@ class Server:
     ``large_pack``. A pack returns when its slowest member is done, so small
     requests would otherwise wait for the largest molecule admitted with
     them. Small requests may use an idle large slot while no large request
-    is queued.
+    is queued. With ``order="size"`` each lane admits its smallest request
+    first, and a pack takes only requests of at most twice its head's size
+    (shortest job first: the percentiles of a burst of mixed sizes drop, the
+    largest requests finish last).
     """
 
     LANES = ("large", "small")
 
     def __init__(self, executor, *, hbm_budget: float = 120e9, slots: int = 8, max_pack: int = 32,
                  large_slots: int = 0, large_n: int | None = None, large_pack: int = 4,
-                 clock=time.perf_counter):
+                 order: str = "fifo", clock=time.perf_counter):
         if slots < 1 or max_pack < 1 or large_pack < 1:
             raise ValueError("slots and pack sizes must be positive")
         if not 0 <= large_slots < slots:
@@ -120,6 +123,10 @@ class Server:
         self.large_slots = large_slots
         self.large_n = large_n
         self.large_pack = large_pack
+        if order not in ("fifo", "size"):
+            raise ValueError("order is 'fifo' or 'size'")
+        self.order = order
+        self._sizes: dict[int, int] = {}
         self.clock = clock
         self.t0 = clock()
         self.queues = {"small": deque(), "large": deque()}
@@ -142,8 +149,16 @@ class Server:
     def now(self) -> float:
         return self.clock() - self.t0
 
+    def _size(self, req: Request) -> int:
+        """Orbitals of a request (cached), the scheduling size."""
+        n = self._sizes.get(id(req))
+        if n is None:
+            n = self.ex.norb(req) if hasattr(self.ex, "norb") else len(req.numbers)
+            self._sizes[id(req)] = n
+        return n
+
     def lane(self, req: Request) -> str:
-        if self.large_slots > 0 and self.ex.norb(req) >= self.large_n:
+        if self.large_slots > 0 and self._size(req) >= self.large_n:
             return "large"
         return "small"
 
@@ -194,6 +209,10 @@ class Server:
                 q = self.queues[lane]
                 if not q:
                     continue
+                if self.order == "size":
+                    # shortest first (stable: arrival order among equal sizes)
+                    q = deque(sorted(q, key=self._size))
+                    self.queues[lane] = q
                 if not self.free[lane] and not (lane == "small" and not self.queues["large"]
                                                 and self.free["large"]):
                     continue
@@ -212,10 +231,12 @@ class Server:
                 if nb > free:
                     continue  # wait for memory: in-flight packs will release it
                 cap = self.large_pack if lane == "large" else self.max_pack
+                nhead = self._size(head)
                 take, rest, tot = [], deque(), 0
                 while q:
                     r = q.popleft()
-                    if len(take) < cap and r.method == head.method:
+                    if (len(take) < cap and r.method == head.method
+                            and (self.order != "size" or self._size(r) <= 2 * nhead)):
                         b = nb if r is head else self.ex.nbytes(r)
                         if tot + b <= free:
                             take.append(r)
@@ -315,7 +336,7 @@ class CudaExecutor:
     """
 
     def __init__(self, device="cuda", *, slots: int = 8, etemp: float = 300.0, maxiter: int = 250,
-                 tol: float = 1e-10):
+                 tol: float = 1e-10, priorities: list[int] | None = None):
         import torch
 
         from . import _lib
@@ -325,7 +346,10 @@ class CudaExecutor:
         self.torch = torch
         self.device = torch.device(device)
         self.tables = {m: Tables(m) for m in METHODS}
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        # per-slot stream priority (lower is higher, torch convention); the
+        # library's per-class streams inherit a non-default one
+        prio = priorities or [0] * slots
+        self.streams = [torch.cuda.Stream(self.device, priority=int(prio[i])) for i in range(slots)]
         self.opts = dict(etemp=etemp, maxiter=maxiter, tol=tol)
         self._ws = {}
 
@@ -433,19 +457,23 @@ def main(argv=None) -> None:
     p.add_argument("--large-slots", type=int, default=3, help="slots of the large-molecule lane (0: one lane)")
     p.add_argument("--large-n", type=int, default=320, help="orbitals from which a request is large")
     p.add_argument("--large-pack", type=int, default=4)
+    p.add_argument("--order", default="size", choices=["size", "fifo"])
     a = p.parse_args(argv)
     methods = tuple(a.methods.split(","))
     reqs = poisson_requests(a.requests, a.rate, a.seed, methods=methods, nat_range=tuple(a.nat))
-    ex = CudaExecutor(slots=a.slots)
+    prio = [-100] * (a.slots - a.large_slots) + [0] * a.large_slots  # small lane first
+    ex = CudaExecutor(slots=a.slots, priorities=prio)
     warm_up(ex, a.slots)
     srv = Server(ex, hbm_budget=a.budget_gb * 1e9, slots=a.slots, max_pack=a.max_pack,
-                 large_slots=a.large_slots, large_n=a.large_n, large_pack=a.large_pack)
+                 large_slots=a.large_slots, large_n=a.large_n, large_pack=a.large_pack,
+                 order=a.order)
     out = srv.serve(reqs)
     s = latency_summary(out)
     s.update({
         "rate_hz": a.rate, "nat_range": list(a.nat), "methods": list(methods), "seed": a.seed,
         "slots": a.slots, "max_pack": a.max_pack, "budget_gb": a.budget_gb,
         "large_slots": a.large_slots, "large_n": a.large_n, "large_pack": a.large_pack,
+        "order": a.order,
         "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
         "max_bytes_gb": srv.stats.max_bytes / 1e9,
         "iterations_max": max(r.iterations for r in out),

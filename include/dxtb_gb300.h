@@ -233,7 +233,10 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
  * 8 or 16 CTAs on as many SMs (classes 2-5) that share every O(n^3) phase.
  * min_n[c-1] is the smallest n of class c (non-decreasing); the default is
  * {112, 136, 160, 320, 640}. Clusters need the launch order of dxtb_scf;
- * cluster sizes the GPU cannot place fold into the largest one it can. */
+ * cluster sizes the GPU cannot place fold into the largest one it can.
+ * Each class runs on a stream of its own, forked from the caller's stream:
+ * larger classes get higher stream priorities, unless the caller's stream
+ * has a non-default priority, which every class then inherits. */
 int32_t dxtb_scf_set_size_classes(const int32_t *min_n);
 /* The current thresholds (min_n [5]). */
 int32_t dxtb_scf_get_size_classes(int32_t *min_n);

@@ -135,3 +135,50 @@ def test_large_molecules_vs_oracle():
             assert abs(float(res.energy[i]) - ref.energy) < E_TOL
             gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
             assert np.abs(gi - ref.extra["gradient"].numpy()).max() < F_TOL
+
+
+def test_config1_gfn1_c8n2o2h12():
+    """Config 1: GFN1 single point (E + forces) of the seeded C8N2O2H12."""
+    from dxtb_gb300.workloads import config_molecules
+
+    (num, pos), = config_molecules(1)
+    assert len(num) == 24
+    ref = X.singlepoint("gfn1", num, pos, grad=True, tol=1e-12)
+    c = calc("gfn1", num)
+    p = torch.tensor(pos, device="cuda")
+    assert abs(float(c.get_energy(p)) - ref.energy) < E_TOL
+    assert np.abs(c.get_forces(p).cpu().numpy() + ref.extra["gradient"].numpy()).max() < F_TOL
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_config3_adjoint_forces_vs_oracle_and_fd(method):
+    """Config 3 (30-120 atoms): energies and adjoint forces against the oracle on
+    four molecules of the set, and against central finite differences
+    (h = 1e-4 Bohr) of the GPU energy for a few coordinates."""
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.workloads import config_molecules
+
+    mols = config_molecules(3, count=64)
+    sel = [mols[i] for i in (0, 1, 2, 3)]
+    pb = PackedBatch(tables(method), [m[0] for m in sel], [torch.tensor(m[1]) for m in sel])
+    res = run(pb, forces=True)
+    assert (res.status.cpu() == 0).all()
+    g = res.gradient.cpu().numpy()
+    for i, (num, pos) in enumerate(sel):
+        ref = X.singlepoint(method, num, pos, grad=True, tol=1e-12)
+        assert abs(float(res.energy[i]) - ref.energy) < E_TOL
+        gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
+        assert np.abs(gi - ref.extra["gradient"].numpy()).max() < F_TOL
+    # finite differences of the GPU energy, molecule 0
+    num, pos = sel[0]
+    h = 1e-4
+    g0 = g[pb.atom_off[0] : pb.atom_off[1]]
+    for a, x in [(0, 0), (len(num) // 2, 1), (len(num) - 1, 2)]:
+        e = []
+        for sgn in (1, -1):
+            q = pos.copy()
+            q[a, x] += sgn * h
+            pbi = PackedBatch(tables(method), [num], [torch.tensor(q)])
+            e.append(float(run(pbi).energy[0]))
+        assert abs((e[0] - e[1]) / (2 * h) - g0[a, x]) < F_TOL

@@ -135,6 +135,23 @@ def test_large_lane_keeps_small_requests_moving():
     assert max(done[10 + i] for i in range(12)) < done[2]
 
 
+def test_size_order_packs_similar_sizes_smallest_first():
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    srv = Server(ex, hbm_budget=1e12, slots=1, max_pack=8, order="size", clock=clk)
+    for rid, nat in enumerate([40, 10, 30, 12, 25, 100]):
+        srv.submit(_req(rid, nat=nat))
+    srv.pump()
+    # smallest head (nat 10 -> 20 orbitals); only requests of <= 40 orbitals join
+    assert ex.launched[0][0] == [1, 3]
+    done = []
+    while not srv.idle:
+        done += srv.pump()
+        clk.t += 0.2
+    order = [ids for ids, _, _ in ex.launched]
+    assert order[1:] == [[4, 2, 0], [5]]  # head 25 atoms (50 orbitals): up to 100 join
+
+
 def test_small_requests_borrow_idle_large_slots():
     clk = FakeClock()
     ex = FakeExecutor(clk)
