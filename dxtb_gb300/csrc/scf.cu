@@ -27,6 +27,9 @@ constexpr double kOccCut = 1e-15;    // orbitals below this occupation carry no 
 constexpr int kLuSlots = 1024;       // concurrent inverse-iteration factorisations per molecule
 constexpr int kClasses = 6;          // size classes: 0 small, 1 one SM, 2..5 clusters of 2..16
 constexpr int kMaxCluster = 16;
+// dynamic shared memory (32 n bytes) next to ~44 KB of static arrays (the
+// one-warp Householder tail among them), within the 227 KB of a CTA
+constexpr int kMaxDynSmem = 180 * 1024;
 
 struct MolView {
   int m, n, nat, nsh, N;
@@ -810,7 +813,7 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
   if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
   const int nmax = a.b.max_nao;
   const size_t smem = (size_t)nmax * (3 * sizeof(double) + 2 * sizeof(float));
-  if (smem > 200 * 1024) return DXTB_ERR_TOO_LARGE;
+  if (smem > kMaxDynSmem) return DXTB_ERR_TOO_LARGE;
   // clusters need the launch order; classes beyond the cluster cap fold down
   int top = a.order ? 5 : 1;
   if (top > 1 && scf_class(a.thr, nmax) >= 2) {
@@ -835,8 +838,8 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
   }
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_scf<kScfThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_scf<kScfThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+    cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
     attr = true;
   }
   // largest classes first: clusters, then one-SM CTAs, then the shared SMs
