@@ -52,6 +52,7 @@ _SIGS = {
     "dxtb_scf": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, f64,
                        vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "dxtb_gradient": (i32, [vp] * 22),
+    "dxtb_scf_gradient": (i32, [vp] * 15 + [f64, i32, f64] + [vp] * 21),
     "dxtb_index_sizes": (i32, [vp, i32, i32, i32, vp, vp, vp]),
     "dxtb_index_maps": (i32, [vp, i32, i32, i32, vp, vp, i64, i64] + [vp] * 14 + [vp]),
     "dxtb_scf_set_size_classes": (i32, [vp]),

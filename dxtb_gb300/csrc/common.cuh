@@ -67,6 +67,25 @@ __device__ __forceinline__ double block_max(double v, double *red) {
   return r;
 }
 
+// Size classes of the SCF launch (smallest n of classes 1..5); a filter
+// restricts a kernel to the molecules of one class (cls < 0: all).
+constexpr int kClasses = 6;
+struct ClassFilter {
+  int thr[kClasses];
+  int cls;
+};
+
+__host__ __device__ inline int scf_class(const int *thr, int n) {
+  int c = 0;
+  for (int k = 1; k < kClasses; ++k)
+    if (n >= thr[k]) c = k;
+  return c;
+}
+
+__device__ __forceinline__ bool in_class(const ClassFilter &f, const dxtb_batch &b, int m) {
+  return f.cls < 0 || scf_class(f.thr, (int)(b.ao_off[m + 1] - b.ao_off[m])) == f.cls;
+}
+
 // SM count of the current device, cached per device (host side).
 inline int32_t device_sms(int *sms) {
   static int cache[64] = {0};
@@ -91,5 +110,13 @@ __device__ __forceinline__ int find_mol(const int64_t *off, int nmol, int64_t k)
   }
   return lo;
 }
+
+// Nuclear-gradient kernels of the molecules selected by a filter (gradient.cu).
+int32_t launch_gradient(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
+                        const double *cn, const double *mrad, const double *density,
+                        const double *wdensity, const double *q, const double *dp, const double *qp,
+                        const double *vorb, const double *vdp, const double *vqp,
+                        const double *overlap, const double *dipole, double *dedcn, double *grad,
+                        const ClassFilter &f, cudaStream_t st);
 
 }  // namespace dxtb

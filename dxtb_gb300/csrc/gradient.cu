@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(gWarps * 32)
                  const double *__restrict__ W, const double *__restrict__ S,
                  const double *__restrict__ D, const double *__restrict__ vorb,
                  const double *__restrict__ vdp, const double *__restrict__ vqp, int multipole,
-                 double *__restrict__ dedcn, double *__restrict__ grad) {
+                 double *__restrict__ dedcn, double *__restrict__ grad, ClassFilter flt) {
   extern __shared__ double smem[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *s_tab = smem + (size_t)w * (gChunk * gTab + 2 * gNComp * 36);
@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(gWarps * 32)
   // grid-stride over shell pairs; the exact count is read on the device
   const int64_t npairs = b.pair_off[b.nmol];
   for (int64_t k = (int64_t)blockIdx.x * gWarps + w; k < npairs; k += (int64_t)gridDim.x * gWarps) {
+    if (flt.cls >= 0 && !in_class(flt, b, find_mol(b.pair_off, b.nmol, k))) continue;  // warp-uniform
     grad_pair(b, pf_, pi_tab, cn, P, W, S, D, vorb, vdp, vqp, multipole, dedcn, grad, k, lane, s_tab,
               s_esph, s_ecart);
     __syncwarp();  // the next pair reuses this warp's shared tables
@@ -355,9 +356,11 @@ __global__ void k_grad_mol(dxtb_batch b, const double *__restrict__ pf_,
                            const int32_t *__restrict__ pi_tab, const double *__restrict__ cn,
                            const double *__restrict__ mrad, const double *__restrict__ q,
                            const double *__restrict__ dp, const double *__restrict__ qp,
-                           int multipole, double *__restrict__ dedcn, double *__restrict__ grad) {
+                           int multipole, double *__restrict__ dedcn, double *__restrict__ grad,
+                           ClassFilter flt) {
   extern __shared__ double sm[];
   const int m = blockIdx.x;
+  if (!in_class(flt, b, m)) return;
   const int64_t a0 = b.atom_off[m], s0 = b.shell_off[m], o0 = b.ao_off[m];
   const int nat = (int)(b.atom_off[m + 1] - a0), nsh = (int)(b.shell_off[m + 1] - s0);
   const int cn_kind = pi_(pi_tab, DXTB_I_SCAL + DXTB_IS_CN_KIND);
@@ -536,22 +539,17 @@ using namespace dxtb;
 
 constexpr size_t gSmem = sizeof(double) * gWarps * (gChunk * gTab + 2 * gNComp * 36);
 
-extern "C" int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
-                                 const double *cn, const double *cn_mp, const double *mrad,
-                                 const double *density, const double *wdensity, const double *q,
-                                 const double *dp, const double *qp, const double *vorb,
-                                 const double *vdp, const double *vqp, const double *overlap,
-                                 const double *dipole, const double *unused0,
-                                 const double *unused1, double *dedcn, double *dedcn_mp,
-                                 double *grad, void *stream) {
-  (void)cn_mp;
-  (void)unused0;
-  (void)unused1;
-  (void)dedcn_mp;
+namespace dxtb {
+
+int32_t launch_gradient(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
+                        const double *cn, const double *mrad, const double *density,
+                        const double *wdensity, const double *q, const double *dp, const double *qp,
+                        const double *vorb, const double *vdp, const double *vqp,
+                        const double *overlap, const double *dipole, double *dedcn, double *grad,
+                        const ClassFilter &f, cudaStream_t st) {
   if (!b || b->nmol <= 0 || !cn || !density || !wdensity || !q || !vorb || !overlap || !dedcn ||
       !grad)
     return DXTB_ERR_ARGS;
-  cudaStream_t st = (cudaStream_t)stream;
   // The multipole (GFN2) terms are taken iff the dipole integrals are given.
   const int multipole = dipole != nullptr;
   if (multipole && (!vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
@@ -567,13 +565,34 @@ extern "C" int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f, const
     const int64_t blocks = min((bound + gWarps - 1) / gWarps, (int64_t)sms * 16);
     k_grad_pairs<<<(unsigned)blocks, gWarps * 32, gSmem, st>>>(*b, par_f, par_i, cn, density, wdensity,
                                                                overlap, dipole, vorb, vdp, vqp, multipole,
-                                                               dedcn, grad);
+                                                               dedcn, grad, f);
     DXTB_CHECK_LAUNCH();
   }
   const size_t smem = sizeof(double) * (size_t)(b->max_nsh + 3 * b->max_nat + 8);
   if (smem > 200 * 1024) return DXTB_ERR_TOO_LARGE;
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_grad_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_grad_mol<<<b->nmol, 128, smem, st>>>(*b, par_f, par_i, cn, mrad, q, dp, qp, multipole, dedcn, grad);
+  k_grad_mol<<<b->nmol, 128, smem, st>>>(*b, par_f, par_i, cn, mrad, q, dp, qp, multipole, dedcn, grad, f);
   DXTB_CHECK_LAUNCH();
   return DXTB_OK;
+}
+
+}  // namespace dxtb
+
+extern "C" int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
+                                 const double *cn, const double *cn_mp, const double *mrad,
+                                 const double *density, const double *wdensity, const double *q,
+                                 const double *dp, const double *qp, const double *vorb,
+                                 const double *vdp, const double *vqp, const double *overlap,
+                                 const double *dipole, const double *unused0,
+                                 const double *unused1, double *dedcn, double *dedcn_mp,
+                                 double *grad, void *stream) {
+  (void)cn_mp;
+  (void)unused0;
+  (void)unused1;
+  (void)dedcn_mp;
+  ClassFilter all;
+  for (int c = 0; c < kClasses; ++c) all.thr[c] = 0;
+  all.cls = -1;
+  return launch_gradient(b, par_f, par_i, cn, mrad, density, wdensity, q, dp, qp, vorb, vdp, vqp,
+                         overlap, dipole, dedcn, grad, all, (cudaStream_t)stream);
 }

@@ -25,7 +25,7 @@ constexpr int kRank = 256;           // Broyden memory (the reference keeps ever
 constexpr double kDamp = 0.5;        // step damping of the root solver (defaults.DAMP)
 constexpr double kOccCut = 1e-15;    // orbitals below this occupation carry no density
 constexpr int kLuSlots = 1024;       // concurrent inverse-iteration factorisations per molecule
-constexpr int kClasses = 6;          // size classes: 0 small, 1 one SM, 2..5 clusters of 2..16
+// size classes (kClasses, common.cuh): 0 small, 1 one SM, 2..5 clusters of 2..16
 constexpr int kMaxCluster = 16;
 // dynamic shared memory (32 n bytes) next to ~44 KB of static arrays (the
 // one-warp Householder tail among them), within the 227 KB of a CTA
@@ -152,14 +152,6 @@ struct ScfArgs {
   int32_t *status;
   int thr[kClasses];  // smallest n of each size class (thr[0] = 0)
 };
-
-// Size class of a molecule with n orbitals.
-__host__ __device__ inline int scf_class(const int *thr, int n) {
-  int c = 0;
-  for (int k = 1; k < kClasses; ++k)
-    if (n >= thr[k]) c = k;
-  return c;
-}
 
 // Potential x = (vorb [n], vdp [nat][3], vqp [nat][6]) from the orbital
 // charges qo and atomic multipoles dpa/qpa (interactions/base.py:135-181).
@@ -804,7 +796,23 @@ static int cluster_cap(size_t smem) {
   return cap;
 }
 
-static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
+// Inputs of the gradient that the SCF arguments do not hold.
+struct GradArgs {
+  const double *cn, *mrad;
+  double *dedcn, *grad;
+};
+
+// The gradient kernels of class c, on the stream of that class's SCF launch.
+static int32_t class_gradient(const ScfArgs &a, const GradArgs *g, int c, cudaStream_t s) {
+  if (g == nullptr) return DXTB_OK;
+  ClassFilter f;
+  for (int k = 0; k < kClasses; ++k) f.thr[k] = a.thr[k];
+  f.cls = c;
+  return launch_gradient(&a.b, a.pf, a.pi, g->cn, g->mrad, a.P, a.W, a.q, a.dp, a.qp, a.vorb, a.vdp,
+                         a.vqp, a.S, a.D, g->dedcn, g->grad, f, s);
+}
+
+static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *g = nullptr) {
   {
     std::lock_guard<std::mutex> lock(g_policy_mutex);
     for (int c = 0; c < kClasses; ++c) a.thr[c] = g_thr[c];
@@ -858,14 +866,22 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, k_scf_cluster, a, c) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    const int32_t rc = class_gradient(a, g, c, cfg.stream);
+    if (rc != DXTB_OK) return rc;
   }
   if (cmax >= 1) {
     k_scf<kScfBigThreads, 1><<<nmol, kScfBigThreads, smem, ss ? ss->s[1] : st>>>(a, 1);
     DXTB_CHECK_LAUNCH();
+    const int32_t rc = class_gradient(a, g, 1, ss ? ss->s[1] : st);
+    if (rc != DXTB_OK) return rc;
   }
   const size_t smem0 = (size_t)min(nmax, a.thr[1]) * (3 * sizeof(double) + 2 * sizeof(float));
   k_scf<kScfThreads, 2><<<nmol, kScfThreads, smem0, ss ? ss->s[0] : st>>>(a, 0);
   DXTB_CHECK_LAUNCH();
+  {
+    const int32_t rc = class_gradient(a, g, 0, ss ? ss->s[0] : st);
+    if (rc != DXTB_OK) return rc;
+  }
   if (ss) {
     for (int c = 0; c <= cmax; ++c) {
       if (cudaEventRecord(ss->join[c], ss->s[c]) != cudaSuccess) return DXTB_ERR_LAUNCH;
@@ -944,6 +960,61 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   a.energies = energies;
   a.status = status;
   return launch_scf(a, b->nmol, (cudaStream_t)stream);
+}
+
+extern "C" int32_t dxtb_scf_gradient(
+    const dxtb_batch *b, const double *par_f, const int32_t *par_i, const double *overlap,
+    const double *h0, const double *dipole, const double *quadrupole, const double *gamma,
+    const double *hd, const double *amat_sd, const double *amat_dd, const double *amat_sq,
+    const double *gb_mat, const double *n0, const double *nel, double kt, int32_t maxiter, double tol,
+    const int64_t *ws_off, const int32_t *order, double *workspace, double *density,
+    double *wdensity, double *coeff, double *evals, double *occ, double *q, double *dp, double *qp,
+    double *vorb, double *vdp, double *vqp, double *energies, int32_t *status, const double *cn,
+    const double *mrad, double *dedcn, double *grad, void *stream) {
+  if (!b || b->nmol <= 0 || !overlap || !h0 || !gamma || !hd || !n0 || !nel || !ws_off ||
+      !workspace || !density || !wdensity || !coeff || !evals || !occ || !q || !vorb || !energies ||
+      !status || !cn || !dedcn || !grad)
+    return DXTB_ERR_ARGS;
+  if (maxiter <= 0 || !(kt > 0.0)) return DXTB_ERR_ARGS;
+  if (dipole != nullptr && (!vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
+  ScfArgs a;
+  a.b = *b;
+  a.pf = par_f;
+  a.pi = par_i;
+  a.S = overlap;
+  a.H0 = h0;
+  a.D = dipole;
+  a.Q = quadrupole;
+  a.gamma = gamma;
+  a.hd = hd;
+  a.sd = amat_sd;
+  a.dd = amat_dd;
+  a.sq = amat_sq;
+  a.gb = gb_mat;
+  a.n0 = n0;
+  a.nel = nel;
+  a.kt = kt;
+  a.xtol = tol;
+  a.ftol = tol;
+  a.maxiter = maxiter;
+  a.ws_off = ws_off;
+  a.order = order;
+  a.ws = workspace;
+  a.P = density;
+  a.W = wdensity;
+  a.C = coeff;
+  a.evals = evals;
+  a.occ = occ;
+  a.q = q;
+  a.dp = dp;
+  a.qp = qp;
+  a.vorb = vorb;
+  a.vdp = vdp;
+  a.vqp = vqp;
+  a.energies = energies;
+  a.status = status;
+  GradArgs g{cn, mrad, dedcn, grad};
+  return launch_scf(a, b->nmol, (cudaStream_t)stream, &g);
 }
 
 // ---------------------------------------------------------------------------

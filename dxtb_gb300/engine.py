@@ -300,40 +300,36 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
         s["status"] = status
     ws = buf("ws", tot["ws"])
     kt = etemp * radii.KELVIN2AU
-    mark("scf", 0)
-    _lib.check(
-        L.dxtb_scf(b, pf, pi, S.data_ptr(), H.data_ptr(), _lib.ptr(D), _lib.ptr(Q), gamma.data_ptr(),
-                   hd.data_ptr(), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq), _lib.ptr(gbm),
-                   pb.t["n0"].data_ptr(), pb.t["nel"].data_ptr(), kt, int(maxiter), float(tol),
-                   pb.t["ws_off"].data_ptr(), pb.t["order"].data_ptr(), ws.data_ptr(), P.data_ptr(),
-                   _lib.ptr(W), Cm.data_ptr(), ev.data_ptr(), occ.data_ptr(), q.data_ptr(),
-                   dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(), vdp.data_ptr(), vqp.data_ptr(),
-                   en.data_ptr(), status.data_ptr(), st),
-        "SCF",
-    )
-    launches += scf_launches(L, int(pb.nao.max()))
-    mark("scf", 1)
-    e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
-    e_rep = _seg_sum(erep[:na], pb.t["atom_mol"], pb.nmol)
+    scf_args = (b, pf, pi, S.data_ptr(), H.data_ptr(), _lib.ptr(D), _lib.ptr(Q), gamma.data_ptr(),
+                hd.data_ptr(), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq), _lib.ptr(gbm),
+                pb.t["n0"].data_ptr(), pb.t["nel"].data_ptr(), kt, int(maxiter), float(tol),
+                pb.t["ws_off"].data_ptr(), pb.t["order"].data_ptr(), ws.data_ptr(), P.data_ptr(),
+                _lib.ptr(W), Cm.data_ptr(), ev.data_ptr(), occ.data_ptr(), q.data_ptr(),
+                dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(), vdp.data_ptr(), vqp.data_ptr(),
+                en.data_ptr(), status.data_ptr())
+    n_scf = scf_launches(L, int(pb.nao.max()))
     grad = None
     if forces:
+        # SCF and gradient fused per size class: each class's forces overlap
+        # the SCF of the larger classes (grad and dE/dCN zeroed first)
         grad = buf("grad", 3 * na)
         grad.zero_()
         dedcn = buf("dedcn", na)
-        dedcn_mp = buf("dedcn_mp", na) if mp else None
         dedcn.zero_()
-        if dedcn_mp is not None:
-            dedcn_mp.zero_()
+        mark("scf", 0)
+        _lib.check(L.dxtb_scf_gradient(*scf_args, cn.data_ptr(), _lib.ptr(mrad), dedcn.data_ptr(),
+                                       grad.data_ptr(), st), "SCF and gradient")
+        launches += 3 * n_scf  # per class: SCF, pair adjoint, per-molecule terms
+        mark("scf", 1)
+    else:
+        mark("scf", 0)
+        _lib.check(L.dxtb_scf(*scf_args, st), "SCF")
+        launches += n_scf
+        mark("scf", 1)
+    e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
+    e_rep = _seg_sum(erep[:na], pb.t["atom_mol"], pb.nmol)
+    if forces:
         mark("gradient", 0)
-        _lib.check(
-            L.dxtb_gradient(b, pf, pi, cn.data_ptr(), cn_mp.data_ptr(), _lib.ptr(mrad), P.data_ptr(),
-                            W.data_ptr(), q.data_ptr(), dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(),
-                            vdp.data_ptr(), vqp.data_ptr(), S.data_ptr(), _lib.ptr(D), None, None,
-                            dedcn.data_ptr(), _lib.ptr(dedcn_mp), grad.data_ptr(), st),
-            "gradient",
-        )
-        launches += 2
-        mark("gradient", 1)
         if gb is not None:
             _lib.check(
                 L.dxtb_born_gradient(b, pf, pi, *ga, q.data_ptr(), s["born"].data_ptr(),
@@ -341,6 +337,7 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
                 "generalized Born gradient",
             )
             launches += 1
+        mark("gradient", 1)
         grad = grad[: 3 * na].view(na, 3)
     energy = e4[:, 0] + e4[:, 1] + e_rep
     return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], status[: pb.nmol], grad, s, launches)

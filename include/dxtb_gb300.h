@@ -241,6 +241,29 @@ int32_t dxtb_scf_set_size_classes(const int32_t *min_n);
 /* The current thresholds (min_n [5]). */
 int32_t dxtb_scf_get_size_classes(int32_t *min_n);
 
+/* dxtb_scf followed by dxtb_gradient, fused per size class: the gradient of
+ * a class's molecules is launched on that class's stream right after its
+ * SCF launch, so it overlaps the SCF of the larger classes. Arguments: those
+ * of dxtb_scf (wdensity required), then cn (the Hamiltonian coordination
+ * numbers), mrad (GFN2 damping radii, else NULL), dedcn [natoms] and grad
+ * [natoms][3], both zeroed by the caller before the call. No counterpart in
+ * the reference (its forces are autograd after the SCF). */
+int32_t dxtb_scf_gradient(const dxtb_batch *b, const double *par_f,
+                          const int32_t *par_i, const double *overlap,
+                          const double *h0, const double *dipole,
+                          const double *quadrupole, const double *gamma,
+                          const double *hd, const double *amat_sd,
+                          const double *amat_dd, const double *amat_sq,
+                          const double *gb_mat, const double *n0,
+                          const double *nel, double kt, int32_t maxiter, double tol,
+                          const int64_t *ws_off, const int32_t *order,
+                          double *workspace, double *density, double *wdensity,
+                          double *coeff, double *evals, double *occ, double *q,
+                          double *dp, double *qp, double *vorb, double *vdp,
+                          double *vqp, double *energies, int32_t *status,
+                          const double *cn, const double *mrad, double *dedcn,
+                          double *grad, void *stream);
+
 /* Nuclear gradient dE/dR [natoms][3] at the converged SCF (analytic
  * adjoint; the reference differentiates with autograd through
  * calculators/types/autograd.py:84-196 and scf/implicit/fixed_point.py).
