@@ -231,168 +231,276 @@ __device__ void team_trinv(Team<CL> &tm, int n, const double *L, double *X) {
   tm.sync();
 }
 
+// Distributed shared memory of a cluster: the address of a shared variable
+// in the CTA of rank r, and stores / loads through it.
+__device__ __forceinline__ uint32_t dsmem_addr(const void *p, int r) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  uint32_t o;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(o) : "r"(a), "r"(r));
+  return o;
+}
+__device__ __forceinline__ void dsmem_st(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ double dsmem_ld(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+
+// v stored into the shared variable *p of every CTA of the team.
+template <bool CL>
+__device__ __forceinline__ void team_push(const Team<CL> &tm, double *p, double v) {
+  if constexpr (CL) {
+    for (int r = 0; r < tm.size; ++r) dsmem_st(dsmem_addr(p, r), v);
+  } else {
+    *p = v;
+  }
+}
+
+__device__ __forceinline__ bool is_neg(double v) { return __double_as_longlong(v) < 0; }
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ double flip_sign(double v) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+}
+
+// Scalars of the Householder reflector of a column (alpha, x) with
+// sg = |x|^2: beta = -sign(alpha) sqrt(alpha^2 + sg), t = (beta - alpha) / beta
+// = 1 + |alpha| / |beta| and scale = 1 / (alpha - beta); sg = 0 gives the
+// identity (t = 0, beta = alpha). A float64 operation costs ~1/64 of a float32
+// one on this part and this chain is serial, so 1/sqrt and the reciprocal
+// start from float32 seeds (~2^-23) refined by two Newton-Raphson steps each
+// in float64 (y <- y + y (1 - x y^2) / 2 for x^-1/2, y <- y + y (1 - s y)
+// for s^-1: quadratic convergence to float64 accuracy) instead of the
+// float64 square root and two divisions; squares outside [2^-120, 2^120]
+// take the float64 sqrt and division.
+__device__ __forceinline__ void householder_scalars(double alpha, double sg, double &t, double &beta,
+                                                    double &scale) {
+  if (is_zero(sg)) {
+    t = 0.0;
+    beta = alpha;
+    scale = 0.0;
+    return;
+  }
+  const double x = fma(alpha, alpha, sg);
+  const double aa = fabs(alpha);
+  const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  double nrm, rs;
+  if (ex > 1023 - 120 && ex < 1023 + 120) {
+    double y = (double)rsqrtf((float)x);
+    double h = fma(-x * y, y, 1.0);
+    y = fma(0.5 * y, h, y);
+    h = fma(-x * y, y, 1.0);
+    y = fma(0.5 * y, h, y);
+    nrm = x * y;
+    t = fma(aa, y, 1.0);
+    const double s = aa + nrm;
+    double r = (double)(1.0f / (float)s);
+    double g = fma(-s, r, 1.0);
+    r = fma(r, g, r);
+    g = fma(-s, r, 1.0);
+    rs = fma(r, g, r);
+  } else {
+    nrm = sqrt(x);
+    t = (aa + nrm) / nrm;
+    rs = 1.0 / (aa + nrm);
+  }
+  // alpha >= 0: beta = -nrm, alpha - beta = |alpha| + nrm; else the opposite signs
+  beta = is_neg(alpha) ? nrm : flip_sign(nrm);
+  scale = is_neg(alpha) ? flip_sign(rs) : rs;
+}
+
 // Householder reduction of a full symmetric matrix to tridiagonal form
 // (lower variant): A = Q T Q^T. On exit d, e hold the diagonal and
 // sub-diagonal (e[i] couples i and i+1), the reflector of step k is stored
-// in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k]; d, e, tau
-// are written by the lead CTA. Every CTA holds the column u of step k, then
-// the Householder vector v and p = t A22 v - K v in shared memory (su, sv,
-// sp: n doubles each), and owns one contiguous chunk of the trailing rows:
-// it forms those entries of A22 v and applies the rank-2 update to those
-// rows. The scalars of a step (column norm, beta, t, K) are formed by warp 0
-// alone from warp partials (fixed order) and broadcast through shared
-// memory: on this part every float64 operation repeated by all threads
-// costs FP64 pipe time. A one-CTA team captures the next column during the
-// update instead of reloading it. pg: global [n] exchange buffer for p
-// (clusters). spart: shared [kPart].
+// in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k].
+//
+// Row i of A belongs to CTA i mod size for the whole reduction: the CTA
+// keeps its rows in shared memory when `srows` has room for them
+// (ceil(n / size) * n doubles, `rows_cap`), else in place in A (one CTA: in
+// place, served by the L1). It alone reads and updates them. Per step k
+// (trailing order m = n - k - 1; u the column below the diagonal, held by
+// every CTA in su):
+//   A. warp 0 forms |u_1..|^2 and the reflector scalars while the other
+//      warps form q~_c = sum_{own r >= 1} A22[r][c] u_r (coalesced over c;
+//      by symmetry these are the own rows' share of A22 u);
+//   B. q = scale q~ + A22[0][c] (the row of v_0 = 1, on its owner), v = scale u
+//      (sv), the own share of v^T A22 v; q (sq) stays in this CTA's shared
+//      memory, the v.q partial is pushed to every CTA;
+//   --- team barrier ---
+//   C. p = t sum_rank q_rank (read from every CTA's shared memory, rank
+//      order: the same bits everywhere), K = t^2/2 sum_rank (v.q)_rank,
+//      w = p - K v (sp);
+//   D. A22[r][c] -= v_r w_c + w_r v_c on the own rows; the new column 0
+//      (the next step's u) is pushed to every CTA's su;
+//   --- team barrier ---
+// so a step moves only vectors between the CTAs (distributed shared memory,
+// no global round trip) and keeps two team barriers. The scalars are
+// computed redundantly by warp 0 of every CTA from identical inputs.
+// su, sv, sp, sq: shared [n]; spart: shared [kPart].
 template <bool CL>
 __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *e, double *tau,
-                             double *pg, double *su, double *sv, double *sp, double *spart) {
-  __shared__ double swarp[32], swarp2[32], sscal[4];
+                             double *su, double *sv, double *sp, double *sq, double *spart,
+                             double *srows, int64_t rows_cap) {
+  __shared__ double swarp[32], sscal[4], skq[16];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
-  bool have_col = false;  // one-CTA team: su and swarp already hold this step's column
+  const int C = tm.size, rk = tm.rank;
+  const int nown = (n + C - 1) / C;  // the same bound on every CTA
+  double *R;
+  size_t ldr;
+  if (srows != nullptr && (int64_t)nown * n <= rows_cap) {
+    R = srows;
+    ldr = (size_t)n;
+    for (int64_t t = threadIdx.x; t < (int64_t)nown * n; t += blockDim.x) {
+      const int j = (int)(t / n), c = (int)(t % n), i = rk + C * j;
+      if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
+    }
+    __syncthreads();
+  } else {
+    R = A + (size_t)rk * n;
+    ldr = (size_t)C * n;
+  }
+  auto rowp = [&](int i) -> double * { return R + (size_t)((i - rk) / C) * ldr; };  // own global row i
+  // column 0 below the diagonal
+  for (int i = rk + C * threadIdx.x; i < n; i += C * blockDim.x)
+    if (i >= 1) team_push(tm, su + (i - 1), rowp(i)[0]);
+  tm.sync();
+  const int nmw = max(1, nty - 1);  // warps of the matvec (warp 0: the scalars)
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
-    if (CL || !have_col) {
-      // the column below the diagonal and the warp partials of its norm
-      double part = 0.0;
-      for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        const double x = ld<CL>(A + (size_t)(k + 1 + r) * n + k);
-        su[r] = x;
-        if (r > 0) part = fma(x, x, part);
-      }
-      part = warp_sum(part);
-      if (tx == 0) swarp[ty] = part;
-      __syncthreads();
-    }
+    const int rb = ((rk - (k + 1)) % C + C) % C;          // first own local row
+    const int mc = rb < m ? (m - rb + C - 1) / C : 0;      // own local rows rb + C jj
+    auto lrow = [&](int jj) -> double * { return rowp(k + 1 + rb + C * jj) + (k + 1); };
+    if (threadIdx.x == 0 && k % C == rk) d[k] = rowp(k)[k];
+    // ---- A ----
+    const int ncg = (m + 31) >> 5;
+    const int nrg = max(1, nmw / ncg);
     if (ty == 0) {
-      double sg = tx < nty ? swarp[tx] : 0.0;
-      sg = warp_sum(sg);  // butterfly order: the same value on every CTA
+      double p0 = 0.0, p1 = 0.0;
+      int r = 1 + tx;
+      for (; r + 32 < m; r += 64) {
+        p0 = fma(su[r], su[r], p0);
+        p1 = fma(su[r + 32], su[r + 32], p1);
+      }
+      if (r < m) p0 = fma(su[r], su[r], p0);
+      const double sg = warp_sum(p0 + p1);
       if (tx == 0) {
-        const double alpha = su[0];
-        double t = 0.0, beta = alpha, scale = 0.0, u0 = 0.0;
-        if (sg > 0.0) {
-          const double nrm = sqrt(alpha * alpha + sg);
-          beta = alpha >= 0.0 ? -nrm : nrm;
-          t = (beta - alpha) / beta;
-          u0 = alpha - beta;  // v = scale * (u0, u_1, u_2, ...)
-          scale = 1.0 / u0;
-        }
+        double t, beta, scale;
+        householder_scalars(su[0], sg, t, beta, scale);
         sscal[0] = t;
         sscal[1] = scale;
-        sscal[2] = u0;
         if (tm.lead()) {
           tau[k] = t;
           e[k] = beta;
-          d[k] = ld<CL>(A + (size_t)k * n + k);
+        }
+      }
+    }
+    if (ty >= 1 || nty == 1) {
+      for (int it = (nty == 1 ? 0 : ty - 1); it < ncg * nrg; it += nmw) {
+        const int cg = it % ncg, rg = it / ncg, c = cg * 32 + tx;
+        double a0 = 0.0, a1 = 0.0;
+        if (c < m) {
+          int jj = rg;
+          if (rb + C * jj == 0) jj += nrg;  // row 0: v_0 = 1, added in B
+          for (; jj + nrg < mc; jj += 2 * nrg) {
+            const int r0 = rb + C * jj, r1 = r0 + C * nrg;
+            a0 = fma(lrow(jj)[c], su[r0], a0);
+            a1 = fma(lrow(jj + nrg)[c], su[r1], a1);
+          }
+          if (jj < mc) a0 = fma(lrow(jj)[c], su[rb + C * jj], a0);
+          if (nrg > 1) spart[rg * m + c] = a0 + a1;
+          else sq[c] = a0 + a1;
         }
       }
     }
     __syncthreads();
-    const double t = sscal[0], scale = sscal[1], u0 = sscal[2];
-    have_col = false;
-    if (t != 0.0) {  // the same on every CTA of the team
-      const int r0 = (int)((int64_t)m * tm.rank / tm.size);
-      const int r1 = (int)((int64_t)m * (tm.rank + 1) / tm.size);
-      const int mc = r1 - r0;
-      double *A22 = A + (size_t)(k + 1) * n + (k + 1);
-      double *pdst = CL ? pg : sp;
-      const double ts = t * scale;
-      // p_r = t (A22 v)_r for the own rows; A22 is symmetric, so row r of the
-      // product reads column r (coalesced over r); the c range is split in G
-      // groups so that all threads work
-      const int G = (mc > 0 && mc < (int)blockDim.x) ? max(1, min(kPart / mc, (int)blockDim.x / mc)) : 1;
-      double kpart = 0.0;  // p . v over the own rows
-      for (int q = threadIdx.x; q < G * mc; q += blockDim.x) {
-        const int rr = q % mc, g = q / mc, r = r0 + rr;
-        double s = g == 0 ? ld<CL>(A22 + r) * u0 : 0.0;
-        for (int c = g == 0 ? G : g; c < m; c += G) s = fma(ld<CL>(A22 + (size_t)c * n + r), su[c], s);
-        if (G > 1) {
-          spart[g * mc + rr] = s;
-        } else {
-          const double pr = ts * s;
-          pdst[r] = pr;
-          kpart = fma(pr, r == 0 ? 1.0 : scale * su[r], kpart);
-        }
+    // ---- B ----
+    const double t = sscal[0], scale = sscal[1];
+    double kq = 0.0;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+      double qt;
+      if (nrg > 1) {
+        qt = spart[c];
+        for (int g = 1; g < nrg; ++g) qt += spart[g * m + c];
+      } else {
+        qt = sq[c];
       }
-      if (G > 1) {
-        __syncthreads();
-        for (int rr = threadIdx.x; rr < mc; rr += blockDim.x) {
-          double s = 0.0;
-          for (int g = 0; g < G; ++g) s += spart[g * mc + rr];
-          const int r = r0 + rr;
-          const double pr = ts * s;
-          pdst[r] = pr;
-          kpart = fma(pr, r == 0 ? 1.0 : scale * su[r], kpart);
-        }
-      }
-      kpart = warp_sum(kpart);
-      if (tx == 0) swarp2[ty] = kpart;
-      __syncthreads();
-      if (ty == 0) {
-        double kk = tx < nty ? swarp2[tx] : 0.0;
-        kk = warp_sum(kk);
-        if (tx == 0) {
-          if constexpr (CL) {
-            double *slot = tm.gred + 16 * (tm.phase & 1);
-            slot[tm.rank] = kk;
-          } else {
-            sscal[3] = 0.5 * t * kk;
-          }
-        }
-      }
+      double q = scale * qt;
+      if (rb == 0) q += lrow(0)[c];
+      const double vc = c == 0 ? 1.0 : scale * su[c];
+      sv[c] = vc;
+      sq[c] = q;
+      kq = fma(q, vc, kq);
+      if (c >= 1 && c >= rb && (c - rb) % C == 0) A[(size_t)(k + 1 + c) * n + k] = vc;
+    }
+    kq = warp_sum(kq);
+    if (tx == 0) swarp[ty] = kq;
+    __syncthreads();
+    if (ty == 0) {
+      double kk = tx < nty ? swarp[tx] : 0.0;
+      kk = warp_sum(kk);
       if constexpr (CL) {
-        double *slot = tm.gred + 16 * (tm.phase & 1);
-        ++tm.phase;
-        tm.sync();  // p and the CTA partials of p.v complete over the team
-        if (threadIdx.x == 0) {
-          double kk = 0.0;
-          for (int c = 0; c < tm.size; ++c) kk += __ldcg(slot + c);
-          sscal[3] = 0.5 * t * kk;
+        if (tx < C) dsmem_st(dsmem_addr(skq + rk, tx), kk);
+      } else {
+        if (tx == 0) sscal[3] = 0.5 * t * t * kk;
+      }
+    }
+    tm.sync();
+    // ---- C ----
+    if constexpr (CL) {
+      if (threadIdx.x == 0) {
+        double kk = skq[0];
+        for (int r = 1; r < C; ++r) kk += skq[r];
+        sscal[3] = 0.5 * t * t * kk;
+      }
+      for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        // loads issued four at a time, summed in rank order
+        double ps = 0.0;
+        for (int r0 = 0; r0 < C; r0 += 4) {
+          double pv[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) pv[r] = r0 + r < C ? dsmem_ld(dsmem_addr(sq + c, r0 + r)) : 0.0;
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (r0 + r < C) ps = (r0 + r == 0) ? pv[r] : ps + pv[r];
         }
+        sp[c] = t * ps;
       }
       __syncthreads();
       const double K = sscal[3];
-      // v and p - K v for all columns; v (own rows) kept in column k
-      for (int c = threadIdx.x; c < m; c += blockDim.x) {
-        const double vc = c == 0 ? 1.0 : scale * su[c];
-        sv[c] = vc;
-        const double pc = CL ? __ldcg(pg + c) : sp[c];
-        sp[c] = fma(-K, vc, pc);
-        if (c >= r0 && c < r1 && c > 0) A[(size_t)(k + 1 + c) * n + k] = vc;
-      }
-      __syncthreads();
-      // rank-2 update of the own rows, columns over lanes (coalesced); a
-      // one-CTA team keeps the updated column 0 (rows >= 1) as the next column
-      double cpart = 0.0;
-      for (int r = r0 + ty; r < r1; r += nty) {
-        const double vr = sv[r], pr = sp[r];
-        double *Wr = A22 + (size_t)r * n;
-        for (int c = tx; c < m; c += 32) {
-          const double nw = fma(-vr, sp[c], fma(-pr, sv[c], ld<CL>(Wr + c)));
-          Wr[c] = nw;
-          if (!CL && c == 0 && r >= 1) {
-            su[r - 1] = nw;
-            if (r >= 2) cpart = fma(nw, nw, cpart);
-          }
-        }
-      }
-      if (!CL) {
-        if (tx == 0) swarp[ty] = cpart;
-        have_col = true;
+      for (int c = threadIdx.x; c < m; c += blockDim.x) sp[c] = fma(-K, sv[c], sp[c]);
+    } else {
+      const double K = sscal[3];
+      for (int c = threadIdx.x; c < m; c += blockDim.x) sp[c] = fma(-K, sv[c], t * sq[c]);
+    }
+    __syncthreads();
+    // ---- D ----
+    for (int it = ty; it < mc * ncg; it += nty) {
+      const int jj = it / ncg, c = (it % ncg) * 32 + tx, r = rb + C * jj;
+      if (c < m) {
+        double *row = lrow(jj);
+        const double nw = fma(-sv[r], sp[c], fma(-sp[r], sv[c], row[c]));
+        row[c] = nw;
+        if (c == 0 && r >= 1) team_push(tm, su + (r - 1), nw);
       }
     }
-    tm.sync();  // the next column is complete
+    tm.sync();  // the next column is complete everywhere
   }
-  if (tm.lead() && threadIdx.x == 0) {
+  if (threadIdx.x == 0) {
     if (n >= 2) {
-      d[n - 2] = ld<CL>(A + (size_t)(n - 2) * n + (n - 2));
-      e[n - 2] = ld<CL>(A + (size_t)(n - 1) * n + (n - 2));
-      tau[n - 2] = 0.0;
+      if ((n - 2) % C == rk) d[n - 2] = rowp(n - 2)[n - 2];
+      if ((n - 1) % C == rk) {
+        e[n - 2] = rowp(n - 1)[n - 2];
+        d[n - 1] = rowp(n - 1)[n - 1];
+      }
+    } else if (rk == 0) {
+      d[0] = R[0];
     }
-    d[n - 1] = ld<CL>(A + (size_t)(n - 1) * n + (n - 1));
-    e[n - 1] = 0.0;
-    tau[n - 1] = 0.0;
+    if (tm.lead()) {
+      if (n >= 2) tau[n - 2] = 0.0;
+      tau[n - 1] = 0.0;
+      e[n - 1] = 0.0;
+    }
   }
   tm.sync();
 }
@@ -413,8 +521,6 @@ __device__ __forceinline__ int sturm_count_f32(int n, const float *d, const floa
   return cnt;
 }
 
-__device__ __forceinline__ bool is_neg(double v) { return __double_as_longlong(v) < 0; }
-__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
 // |v| outside [2^-500, 2^500] (biased exponent test, no FP64 instruction)
 __device__ __forceinline__ bool out_of_range(double v) {
   const int ex = (int)((__double_as_longlong(v) >> 52) & 0x7ff);

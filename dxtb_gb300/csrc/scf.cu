@@ -27,9 +27,10 @@ constexpr double kOccCut = 1e-15;    // orbitals below this occupation carry no 
 constexpr int kLuSlots = 1024;       // concurrent inverse-iteration factorisations per molecule
 // size classes (kClasses, common.cuh): 0 small, 1 one SM, 2..5 clusters of 2..16
 constexpr int kMaxCluster = 16;
-// dynamic shared memory (32 n bytes) next to ~44 KB of static arrays (the
-// one-warp Householder tail among them), within the 227 KB of a CTA
-constexpr int kMaxDynSmem = 180 * 1024;
+// dynamic shared memory: 32 n bytes, plus the rows of the Householder
+// reduction where they fit (one-SM and cluster teams), next to ~10 KB of
+// static arrays, within the 227 KB of a CTA
+constexpr int kMaxDynSmem = 208 * 1024;
 
 struct MolView {
   int m, n, nat, nsh, N;
@@ -399,9 +400,11 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
 }
 
 // The SCF of molecule m_ by the team tm. dsm: dynamic shared memory of
-// 3 n doubles + 2 n floats (n of this molecule or larger).
+// 3 n doubles + 2 n floats (n of this molecule or larger), then room for
+// the rows of the Householder reduction (`rows`: false for teams that
+// share an SM, which keep the rows in the L1).
 template <bool CL>
-__device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
+__device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm, bool rows) {
   __shared__ double red[32];
   __shared__ double spart[kPart];
   const dxtb_batch &b = a.b;
@@ -498,7 +501,13 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm) {
     }
     tm.sync();
     // ---- eigenvalues: Householder tridiagonalisation + bisection/Newton ----
-    team_tridiag(tm, n, w.A, w.d, w.e, w.tau, w.p, sd, se, sw, spart);
+    {
+      uint32_t dyn;
+      asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+      const int64_t cap = (int64_t)(dyn / sizeof(double)) - 4 * (int64_t)n;
+      team_tridiag(tm, n, w.A, w.d, w.e, w.tau, sd, se, sw, reinterpret_cast<double *>(df), spart,
+                   rows && cap > 0 ? dsm + 4 * n : nullptr, cap);
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       sd[i] = ld<CL>(w.d + i);
       se[i] = ld<CL>(w.e + i);
@@ -663,7 +672,7 @@ __global__ void __launch_bounds__(NT, MINB) k_scf(ScfArgs a, int cls) {
   tm.tid = threadIdx.x;
   tm.stid = threadIdx.x;
   tm.nthr = blockDim.x;
-  scf_body<false>(a, m, tm, dsm);
+  scf_body<false>(a, m, tm, dsm, MINB == 1);
 }
 
 // One thread-block cluster per molecule of size class `cls` (2..5); the
@@ -683,7 +692,7 @@ __global__ void __launch_bounds__(kScfBigThreads, 1) k_scf_cluster(ScfArgs a, in
   for (int i = 0; i < a.b.nmol; ++i) {
     const int m = a.order ? a.order[i] : i;
     if (scf_class(a.thr, (int)(a.b.ao_off[m + 1] - a.b.ao_off[m])) != cls) continue;
-    if (cnt++ % nq == q) scf_body<true>(a, m, tm, dsm);
+    if (cnt++ % nq == q) scf_body<true>(a, m, tm, dsm, true);
   }
 }
 
@@ -766,7 +775,7 @@ static int cluster_cap(size_t smem) {
   std::lock_guard<std::mutex> lock(mu);
   if (cap_dev[dev] != 0 && cap_smem[dev] >= smem) return cap_dev[dev];
   if (cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-      cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem) !=
           cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -850,13 +859,21 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
     attr = true;
   }
+  // shared memory of class c: the base plus the rows of the Householder
+  // reduction of its largest possible molecule, when they fit
+  auto class_smem = [&](int c) -> size_t {
+    const int csize = c >= 2 ? 1 << (c - 1) : 1;
+    const int nub = (c + 1 < kClasses && a.thr[c + 1] != INT32_MAX) ? min(nmax, a.thr[c + 1] - 1) : nmax;
+    const size_t full = smem + (size_t)((nub + csize - 1) / csize) * nub * sizeof(double);
+    return full <= (size_t)kMaxDynSmem ? full : smem;
+  };
   // largest classes first: clusters, then one-SM CTAs, then the shared SMs
   for (int c = cmax; c >= 2; --c) {
     const int csize = 1 << (c - 1);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(min(nmol, max(1, sms / csize)) * csize);
     cfg.blockDim = dim3(kScfBigThreads);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = class_smem(c);
     cfg.stream = ss ? ss->s[c] : st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -870,7 +887,7 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     if (rc != DXTB_OK) return rc;
   }
   if (cmax >= 1) {
-    k_scf<kScfBigThreads, 1><<<nmol, kScfBigThreads, smem, ss ? ss->s[1] : st>>>(a, 1);
+    k_scf<kScfBigThreads, 1><<<nmol, kScfBigThreads, class_smem(1), ss ? ss->s[1] : st>>>(a, 1);
     DXTB_CHECK_LAUNCH();
     const int32_t rc = class_gradient(a, g, 1, ss ? ss->s[1] : st);
     if (rc != DXTB_OK) return rc;
