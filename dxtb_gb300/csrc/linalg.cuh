@@ -248,6 +248,28 @@ __device__ __forceinline__ double dsmem_ld(uint32_t a) {
   return v;
 }
 
+// Sum of f(0) .. f(C-1) for C in {1, 2, 4, 8, 16} (the team sizes of the
+// SCF launches) as a fixed pairwise tree:
+// groups of four ((f0 + f1) + (f2 + f3)), then the group sums pairwise.
+template <typename F>
+__device__ __forceinline__ double rank_tree_sum(int C, F f) {
+  if (C == 1) return f(0);
+  if (C == 2) return f(0) + f(1);
+  double g[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (4 * q < C) {
+      const double a = f(4 * q), b = f(4 * q + 1), c = f(4 * q + 2), d = f(4 * q + 3);
+      g[q] = (a + b) + (c + d);
+    } else {
+      g[q] = 0.0;
+    }
+  }
+  if (C == 4) return g[0];
+  if (C == 8) return g[0] + g[1];
+  return (g[0] + g[1]) + (g[2] + g[3]);
+}
+
 // v stored into the shared variable *p of every CTA of the team.
 template <bool CL>
 __device__ __forceinline__ void team_push(const Team<CL> &tm, double *p, double v) {
@@ -264,16 +286,29 @@ __device__ __forceinline__ double flip_sign(double v) {
   return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
 }
 
+// 1/x: a float32 seed y (relative error e0 ~ 2^-22) refined by one
+// third-order Newton-Raphson step y <- y + y (g + g^2), g = 1 - x y (error
+// e0^3, below float64 rounding): three dependent float64 instructions
+// instead of a float64 division (about ten); |x| outside [2^-120, 2^120]
+// takes the division.
+__device__ __forceinline__ double rcp_nr(double x) {
+  const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  if (ex <= 1023 - 120 || ex >= 1023 + 120) return 1.0 / x;
+  const double r = (double)__fdividef(1.0f, (float)x);
+  const double g = fma(-x, r, 1.0);
+  return fma(r, fma(g, g, g), r);
+}
+
 // Scalars of the Householder reflector of a column (alpha, x) with
 // sg = |x|^2: beta = -sign(alpha) sqrt(alpha^2 + sg), t = (beta - alpha) / beta
 // = 1 + |alpha| / |beta| and scale = 1 / (alpha - beta); sg = 0 gives the
-// identity (t = 0, beta = alpha). A float64 operation costs ~1/64 of a float32
-// one on this part and this chain is serial, so 1/sqrt and the reciprocal
-// start from float32 seeds (~2^-23) refined by two Newton-Raphson steps each
-// in float64 (y <- y + y (1 - x y^2) / 2 for x^-1/2, y <- y + y (1 - s y)
-// for s^-1: quadratic convergence to float64 accuracy) instead of the
-// float64 square root and two divisions; squares outside [2^-120, 2^120]
-// take the float64 sqrt and division.
+// identity (t = 0, beta = alpha). A float64 instruction costs a warp ~65
+// cycles on this part and this chain is serial, so 1/sqrt and the reciprocal
+// start from float32 seeds (~2^-23) refined by one third-order
+// Newton-Raphson step each in float64 (x^-1/2: y <- y + y (h/2 + 3 h^2/8),
+// h = 1 - x y^2; s^-1: rcp_nr), whose error (~2^-69) is below float64
+// rounding, instead of the float64 square root and two divisions; squares
+// outside [2^-120, 2^120] take the float64 sqrt and division.
 __device__ __forceinline__ void householder_scalars(double alpha, double sg, double &t, double &beta,
                                                     double &scale) {
   if (is_zero(sg)) {
@@ -287,19 +322,12 @@ __device__ __forceinline__ void householder_scalars(double alpha, double sg, dou
   const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
   double nrm, rs;
   if (ex > 1023 - 120 && ex < 1023 + 120) {
-    double y = (double)rsqrtf((float)x);
-    double h = fma(-x * y, y, 1.0);
-    y = fma(0.5 * y, h, y);
-    h = fma(-x * y, y, 1.0);
-    y = fma(0.5 * y, h, y);
+    const double y0 = (double)rsqrtf((float)x);
+    const double h = fma(-x * y0, y0, 1.0);
+    const double y = fma(y0 * h, fma(h, 0.375, 0.5), y0);
     nrm = x * y;
     t = fma(aa, y, 1.0);
-    const double s = aa + nrm;
-    double r = (double)(1.0f / (float)s);
-    double g = fma(-s, r, 1.0);
-    r = fma(r, g, r);
-    g = fma(-s, r, 1.0);
-    rs = fma(r, g, r);
+    rs = rcp_nr(aa + nrm);
   } else {
     nrm = sqrt(x);
     t = (aa + nrm) / nrm;
@@ -316,27 +344,32 @@ __device__ __forceinline__ void householder_scalars(double alpha, double sg, dou
 // in A[k+2..n-1][k] (its leading 1 implicit) with factor tau[k].
 //
 // Row i of A belongs to CTA i mod size for the whole reduction: the CTA
-// keeps its rows in shared memory when `srows` has room for them
-// (ceil(n / size) * n doubles, `rows_cap`), else in place in A (one CTA: in
-// place, served by the L1). It alone reads and updates them. Per step k
-// (trailing order m = n - k - 1; u the column below the diagonal, held by
-// every CTA in su):
-//   A. warp 0 forms |u_1..|^2 and the reflector scalars while the other
-//      warps form q~_c = sum_{own r >= 1} A22[r][c] u_r (coalesced over c;
-//      by symmetry these are the own rows' share of A22 u);
-//   B. q = scale q~ + A22[0][c] (the row of v_0 = 1, on its owner), v = scale u
-//      (sv), the own share of v^T A22 v; q (sq) stays in this CTA's shared
-//      memory, the v.q partial is pushed to every CTA;
+// keeps its rows in shared memory when `srows` has room for them (and, in a
+// cluster, one more row: (ceil(n / size) + 1) * n doubles, `rows_cap`), else
+// in place in A (one CTA: in place, served by the L1). It alone reads and
+// updates them.
+// Every CTA holds the column u of the step (su) and the reflector scalars
+// (t, scale), formed one step ahead. Per step k (trailing order
+// m = n - k - 1, A22 the trailing matrix):
+//   A. v = scale u (v_0 = 1) into sv; q_c = sum_{own r} A22[r][c] v_r for
+//      all c (coalesced over c; by symmetry the own rows' share of A22 v);
+//   B. the own share of v^T A22 v is pushed to every CTA; the owner of
+//      row 0 of A22 (= column 0, the next column before the update) pushes
+//      it to every CTA as well (rows in shared memory);
 //   --- team barrier ---
-//   C. p = t sum_rank q_rank (read from every CTA's shared memory, rank
+//   C. p = t sum_rank q_rank (read from every CTA's shared memory in rank
 //      order: the same bits everywhere), K = t^2/2 sum_rank (v.q)_rank,
-//      w = p - K v (sp);
-//   D. A22[r][c] -= v_r w_c + w_r v_c on the own rows; the new column 0
-//      (the next step's u) is pushed to every CTA's su;
+//      w = p - K v (sp); the next column u' = (A22 - v w^T - w v^T)[1.., 0]
+//      formed by every CTA from row 0, v and w;
+//   D. warp 0 forms the scalars of step k + 1 from u' while the other warps
+//      update the own rows: A22[r][c] -= v_r w_c + w_r v_c (row 0, which
+//      leaves the trailing matrix, only on its diagonal);
 //   --- team barrier ---
 // so a step moves only vectors between the CTAs (distributed shared memory,
-// no global round trip) and keeps two team barriers. The scalars are
-// computed redundantly by warp 0 of every CTA from identical inputs.
+// no global round trip), keeps two team barriers, and the serial float64
+// chain of the scalars (a warp issues one float64 instruction per ~64
+// cycles) runs beside the update. Quantities formed by every CTA come from
+// identical inputs in identical order, so they agree bit for bit.
 // su, sv, sp, sq: shared [n]; spart: shared [kPart].
 template <bool CL>
 __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *e, double *tau,
@@ -346,11 +379,12 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
   const int C = tm.size, rk = tm.rank;
   const int nown = (n + C - 1) / C;  // the same bound on every CTA
-  double *R;
+  double *R, *sc0 = nullptr;
   size_t ldr;
-  if (srows != nullptr && (int64_t)nown * n <= rows_cap) {
+  if (srows != nullptr && (int64_t)(nown + (CL ? 1 : 0)) * n <= rows_cap) {
     R = srows;
     ldr = (size_t)n;
+    if (CL) sc0 = srows + (size_t)nown * n;
     for (int64_t t = threadIdx.x; t < (int64_t)nown * n; t += blockDim.x) {
       const int j = (int)(t / n), c = (int)(t % n), i = rk + C * j;
       if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
@@ -361,84 +395,95 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
     ldr = (size_t)C * n;
   }
   auto rowp = [&](int i) -> double * { return R + (size_t)((i - rk) / C) * ldr; };  // own global row i
+  // scalars of step k from su[0..m): warp 0 (the lead's lane 0 stores tau, e)
+  auto scalars = [&](int k, int m) {
+    double p0 = 0.0, p1 = 0.0;
+    int r = 1 + tx;
+    for (; r + 32 < m; r += 64) {
+      p0 = fma(su[r], su[r], p0);
+      p1 = fma(su[r + 32], su[r + 32], p1);
+    }
+    if (r < m) p0 = fma(su[r], su[r], p0);
+    const double sg = warp_sum(p0 + p1);
+    if (tx == 0) {
+      double t, beta, scale;
+      householder_scalars(su[0], sg, t, beta, scale);
+      sscal[0] = t;
+      sscal[1] = scale;
+      if (tm.lead()) {
+        tau[k] = t;
+        e[k] = beta;
+      }
+    }
+  };
   // column 0 below the diagonal
   for (int i = rk + C * threadIdx.x; i < n; i += C * blockDim.x)
     if (i >= 1) team_push(tm, su + (i - 1), rowp(i)[0]);
   tm.sync();
-  const int nmw = max(1, nty - 1);  // warps of the matvec (warp 0: the scalars)
+  if (n > 2 && ty == 0) scalars(0, n - 1);
+  __syncthreads();
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
     const int rb = ((rk - (k + 1)) % C + C) % C;          // first own local row
     const int mc = rb < m ? (m - rb + C - 1) / C : 0;      // own local rows rb + C jj
     auto lrow = [&](int jj) -> double * { return rowp(k + 1 + rb + C * jj) + (k + 1); };
     if (threadIdx.x == 0 && k % C == rk) d[k] = rowp(k)[k];
-    // ---- A ----
-    const int ncg = (m + 31) >> 5;
-    const int nrg = max(1, nmw / ncg);
-    if (ty == 0) {
-      double p0 = 0.0, p1 = 0.0;
-      int r = 1 + tx;
-      for (; r + 32 < m; r += 64) {
-        p0 = fma(su[r], su[r], p0);
-        p1 = fma(su[r + 32], su[r + 32], p1);
-      }
-      if (r < m) p0 = fma(su[r], su[r], p0);
-      const double sg = warp_sum(p0 + p1);
-      if (tx == 0) {
-        double t, beta, scale;
-        householder_scalars(su[0], sg, t, beta, scale);
-        sscal[0] = t;
-        sscal[1] = scale;
-        if (tm.lead()) {
-          tau[k] = t;
-          e[k] = beta;
-        }
-      }
-    }
-    if (ty >= 1 || nty == 1) {
-      for (int it = (nty == 1 ? 0 : ty - 1); it < ncg * nrg; it += nmw) {
-        const int cg = it % ncg, rg = it / ncg, c = cg * 32 + tx;
-        double a0 = 0.0, a1 = 0.0;
-        if (c < m) {
-          int jj = rg;
-          if (rb + C * jj == 0) jj += nrg;  // row 0: v_0 = 1, added in B
-          for (; jj + nrg < mc; jj += 2 * nrg) {
-            const int r0 = rb + C * jj, r1 = r0 + C * nrg;
-            a0 = fma(lrow(jj)[c], su[r0], a0);
-            a1 = fma(lrow(jj + nrg)[c], su[r1], a1);
-          }
-          if (jj < mc) a0 = fma(lrow(jj)[c], su[rb + C * jj], a0);
-          if (nrg > 1) spart[rg * m + c] = a0 + a1;
-          else sq[c] = a0 + a1;
-        }
-      }
-    }
-    __syncthreads();
-    // ---- B ----
     const double t = sscal[0], scale = sscal[1];
-    double kq = 0.0;
+    // ---- A ----
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      double qt;
-      if (nrg > 1) {
-        qt = spart[c];
-        for (int g = 1; g < nrg; ++g) qt += spart[g * m + c];
-      } else {
-        qt = sq[c];
-      }
-      double q = scale * qt;
-      if (rb == 0) q += lrow(0)[c];
       const double vc = c == 0 ? 1.0 : scale * su[c];
       sv[c] = vc;
-      sq[c] = q;
-      kq = fma(q, vc, kq);
       if (c >= 1 && c >= rb && (c - rb) % C == 0) A[(size_t)(k + 1 + c) * n + k] = vc;
     }
-    kq = warp_sum(kq);
-    if (tx == 0) swarp[ty] = kq;
+    __syncthreads();
+    const int ncg = (m + 31) >> 5;
+    const int nrg = max(1, nty / ncg);
+    for (int it = ty; it < ncg * nrg; it += nty) {
+      const int cg = it % ncg, rg = it / ncg, c = cg * 32 + tx;
+      if (c < m) {
+        double a0 = 0.0, a1 = 0.0;
+        int jj = rg;
+        for (; jj + nrg < mc; jj += 2 * nrg) {
+          a0 = fma(lrow(jj)[c], sv[rb + C * jj], a0);
+          a1 = fma(lrow(jj + nrg)[c], sv[rb + C * (jj + nrg)], a1);
+        }
+        if (jj < mc) a0 = fma(lrow(jj)[c], sv[rb + C * jj], a0);
+        if (nrg > 1) spart[rg * m + c] = a0 + a1;
+        else sq[c] = a0 + a1;
+      }
+    }
+    __syncthreads();
+    // ---- B ---- (float64 instructions cost pipe time on every warp that
+    // issues them, active lanes or not: only the warps that hold entries of
+    // q take part in the reduction)
+    const int nwq = min(nty, (m + 31) >> 5);
+    double kq = 0.0;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+      double q;
+      if (nrg > 1) {
+        q = spart[c];
+        for (int g = 1; g < nrg; ++g) q += spart[g * m + c];
+        sq[c] = q;
+      } else {
+        q = sq[c];
+      }
+      kq = fma(q, sv[c], kq);
+    }
+    if (CL && sc0 != nullptr && rb == 0 && mc > 0) {
+      const double *row0 = lrow(0);
+      for (int c = 1 + threadIdx.x; c < m; c += blockDim.x) team_push(tm, sc0 + c, row0[c]);
+    }
+    if (ty < nwq) {
+      kq = warp_sum(kq);
+      if (tx == 0) swarp[ty] = kq;
+    }
     __syncthreads();
     if (ty == 0) {
-      double kk = tx < nty ? swarp[tx] : 0.0;
-      kk = warp_sum(kk);
+      // butterfly over the smallest power of two >= nwq lanes only
+      double kk = tx < nwq ? swarp[tx] : 0.0;
+      for (int o = nwq > 1 ? 1 << (31 - __clz(nwq - 1)) : 0; o > 0; o >>= 1)
+        kk += __shfl_xor_sync(0xffffffffu, kk, o);
+      kk = __shfl_sync(0xffffffffu, kk, 0);  // lanes past the group hold partial sums
       if constexpr (CL) {
         if (tx < C) dsmem_st(dsmem_addr(skq + rk, tx), kk);
       } else {
@@ -448,24 +493,10 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
     tm.sync();
     // ---- C ----
     if constexpr (CL) {
-      if (threadIdx.x == 0) {
-        double kk = skq[0];
-        for (int r = 1; r < C; ++r) kk += skq[r];
-        sscal[3] = 0.5 * t * t * kk;
-      }
-      for (int c = threadIdx.x; c < m; c += blockDim.x) {
-        // loads issued four at a time, summed in rank order
-        double ps = 0.0;
-        for (int r0 = 0; r0 < C; r0 += 4) {
-          double pv[4];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) pv[r] = r0 + r < C ? dsmem_ld(dsmem_addr(sq + c, r0 + r)) : 0.0;
-#pragma unroll
-          for (int r = 0; r < 4; ++r)
-            if (r0 + r < C) ps = (r0 + r == 0) ? pv[r] : ps + pv[r];
-        }
-        sp[c] = t * ps;
-      }
+      // sums over the ranks as fixed pairwise trees (depth log2 size)
+      if (threadIdx.x == 0) sscal[3] = 0.5 * t * t * rank_tree_sum(C, [&](int r) { return skq[r]; });
+      for (int c = threadIdx.x; c < m; c += blockDim.x)
+        sp[c] = t * rank_tree_sum(C, [&](int r) { return dsmem_ld(dsmem_addr(sq + c, r)); });
       __syncthreads();
       const double K = sscal[3];
       for (int c = threadIdx.x; c < m; c += blockDim.x) sp[c] = fma(-K, sv[c], sp[c]);
@@ -474,17 +505,37 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
       for (int c = threadIdx.x; c < m; c += blockDim.x) sp[c] = fma(-K, sv[c], t * sq[c]);
     }
     __syncthreads();
-    // ---- D ----
-    for (int it = ty; it < mc * ncg; it += nty) {
-      const int jj = it / ncg, c = (it % ncg) * 32 + tx, r = rb + C * jj;
-      if (c < m) {
-        double *row = lrow(jj);
-        const double nw = fma(-sv[r], sp[c], fma(-sp[r], sv[c], row[c]));
-        row[c] = nw;
-        if (c == 0 && r >= 1) team_push(tm, su + (r - 1), nw);
+    // the next column: u'[r - 1] = A22[0][r] - v_r w_0 - w_r v_0, r >= 1
+    {
+      const double w0 = sp[0], v0 = sv[0];
+      const double *g0 = A + (size_t)(k + 1) * n + (k + 1);  // row 0 of A22 in place
+      const double *l0 = (!CL && mc > 0) ? lrow(0) : nullptr;
+      for (int r = 1 + threadIdx.x; r < m; r += blockDim.x) {
+        const double a0 = CL ? (sc0 != nullptr ? sc0[r] : ld<CL>(g0 + r)) : l0[r];
+        su[r - 1] = fma(-sv[r], w0, fma(-sp[r], v0, a0));
       }
     }
-    tm.sync();  // the next column is complete everywhere
+    __syncthreads();
+    // ---- D ----
+    // warp 0's serial chain keeps its sub-partition's float64 pipe to itself
+    // (warps 4, 8, 12 share it and stay idle; a shared pipe slowed the chain
+    // several fold); the update runs on the warps of the other three
+    if (ty == 0) {
+      if (k + 1 < n - 2) scalars(k + 1, m - 1);
+    } else if ((ty & 3) != 0) {
+      const int nu = nty - ((nty + 3) >> 2), uw = ty - (ty >> 2) - 1;
+      for (int it = uw; it < mc * ncg; it += nu) {
+        const int jj = it / ncg, c = (it % ncg) * 32 + tx, r = rb + C * jj;
+        // row 0 of A22 leaves the trailing matrix: only its diagonal (d of
+        // the next step) is kept; the rest is still being read as the next
+        // column by the other CTAs
+        if (c < m && (r > 0 || c == 0)) {
+          double *row = lrow(jj);
+          row[c] = fma(-sv[r], sp[c], fma(-sp[r], sv[c], row[c]));
+        }
+      }
+    }
+    tm.sync();  // the rows, the next column and its scalars are complete
   }
   if (threadIdx.x == 0) {
     if (n >= 2) {
@@ -505,19 +556,39 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
   tm.sync();
 }
 
-// Number of eigenvalues of the tridiagonal (d, e) below x (Sturm count of
-// the LDL^T pivots, zero pivots replaced by -tiny), in float32.
-__device__ __forceinline__ int sturm_count_f32(int n, const float *d, const float *e2, float x,
-                                               float tiny) {
-  int cnt = 0;
-  float q = d[0] - x;
-  if (q == 0.0f) q = -tiny;
-  cnt += q < 0.0f;
-  for (int i = 1; i < n; ++i) {
-    q = (d[i] - x) - __fdividef(e2[i - 1], q);
-    if (q == 0.0f) q = -tiny;
-    cnt += q < 0.0f;
+// Number of eigenvalues of the tridiagonal below x, in float32 and without
+// divisions: sign changes of the leading principal minors p_k of T - x I
+// (three-term recurrence p_{k+1} = (d_k - x) p_k - e2_{k-1} p_{k-1}, e2 = e^2).
+// A zero minor is replaced by a tiny value of the opposite sign of its
+// predecessor (it counts as a change, like a zero pivot replaced by -tiny).
+// Every fourth row the pair is rescaled by 2^-+64 when the larger magnitude
+// leaves [2^-40, 2^40]. Everything is selects and sign-bit arithmetic: a
+// data-dependent branch per row made the count seven times slower.
+__device__ __forceinline__ int sturm_count_f32(int n, const float *d, const float *e2, float x) {
+  float p0 = 1.0f, p1 = d[0] - x;
+  p1 = p1 == 0.0f ? -1e-30f : p1;
+  int cnt = __float_as_int(p1) < 0 ? 1 : 0;
+  auto step = [&](float dx, float ee) {
+    float p2 = fmaf(dx, p1, -ee * p0);
+    p2 = p2 == 0.0f ? (__float_as_int(p1) < 0 ? 1e-30f : -1e-30f) : p2;
+    cnt += (__float_as_int(p2) ^ __float_as_int(p1)) < 0 ? 1 : 0;
+    p0 = p1;
+    p1 = p2;
+  };
+  int i = 1;
+  for (; i + 3 < n; i += 4) {
+    const float d0 = d[i] - x, d1 = d[i + 1] - x, d2 = d[i + 2] - x, d3 = d[i + 3] - x;
+    const float f0 = e2[i - 1], f1 = e2[i], f2 = e2[i + 1], f3 = e2[i + 2];
+    step(d0, f0);
+    step(d1, f1);
+    step(d2, f2);
+    step(d3, f3);
+    const int em = max((__float_as_int(p1) >> 23) & 0xff, (__float_as_int(p0) >> 23) & 0xff);
+    const float sc = em > 127 + 40 ? 0x1p-64f : (em < 127 - 40 ? 0x1p64f : 1.0f);
+    p0 *= sc;
+    p1 *= sc;
   }
+  for (; i < n; ++i) step(d[i] - x, e2[i - 1]);
   return cnt;
 }
 
@@ -530,29 +601,27 @@ __device__ __forceinline__ bool out_of_range(double v) {
 // The same count in float64 without divisions: the pivots of T - x I are
 // q_k = p_k / p_{k-1} for the leading principal minors p_k = det(T_k - x I)
 // (three-term recurrence, e2 = e^2), so a negative pivot is a sign change
-// between p_{k-1} and p_k. A zero minor counts as a change, like a zero
-// pivot replaced by -tiny, and continues as a tiny value of that sign; the
-// pair (p_{k-1}, p_k) is rescaled (every 8 steps) to stay in range.
+// between p_{k-1} and p_k. A zero minor counts as a change and continues as a
+// tiny value of the opposite sign of its predecessor; every eighth row the
+// pair is rescaled (by 2^-+500) to stay in range. Selects and sign bits
+// only, no data-dependent branch.
 __device__ __forceinline__ int sturm_count_f64(int n, const double *d, const double *e2, double x) {
   double p0 = 1.0, p1 = d[0] - x;
-  bool neg1 = is_neg(p1) || is_zero(p1);
-  if (is_zero(p1)) p1 = -1e-300;
-  int cnt = neg1 ? 1 : 0;
+  p1 = is_zero(p1) ? -1e-300 : p1;
+  int cnt = is_neg(p1) ? 1 : 0;
   for (int i = 1; i < n; ++i) {
     double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
-    bool neg2 = is_neg(p2);
-    if (is_zero(p2)) {
-      neg2 = !neg1;
-      p2 = neg2 ? -1e-300 : 1e-300;
-    }
-    cnt += neg2 != neg1;
-    neg1 = neg2;
+    p2 = is_zero(p2) ? (is_neg(p1) ? 1e-300 : -1e-300) : p2;
+    cnt += (__double_as_longlong(p2) ^ __double_as_longlong(p1)) < 0 ? 1 : 0;
     p0 = p1;
     p1 = p2;
-    if ((i & 7) == 0 && (out_of_range(p0) || out_of_range(p1))) {
-      const double sc = (fabs(p1) + fabs(p0)) > 1.0 ? 0x1p-500 : 0x1p500;
-      p0 *= sc;
-      p1 *= sc;
+    if ((i & 7) == 0) {
+      const int em = max((int)((__double_as_longlong(p1) >> 52) & 0x7ff), (int)((__double_as_longlong(p0) >> 52) & 0x7ff));
+      if (em > 1023 + 500 || em < 1023 - 500) {
+        const double sc = em > 1023 ? 0x1p-500 : 0x1p500;
+        p0 *= sc;
+        p1 *= sc;
+      }
     }
   }
   return cnt;
@@ -577,7 +646,7 @@ __device__ __forceinline__ double charpoly_ratio(int n, const double *d, const d
       p0 *= sc; p1 *= sc; q0 *= sc; q1 *= sc;
     }
   }
-  return q1 != 0.0 ? p1 / q1 : 0.0;
+  return q1 != 0.0 ? p1 * rcp_nr(q1) : 0.0;
 }
 
 // All eigenvalues of the symmetric tridiagonal (d, e) (shared-memory copies
@@ -623,25 +692,45 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
   const double tnorm = fmax(fabs(s_gl), fabs(s_gu));
   const double span = s_gu - s_gl;
   const double glo = s_gl - 1e-6 * span - 1e-12, ghi = s_gu + 1e-6 * span + 1e-12;
-  const float tinyf = 1e-30f;
+  // bound on the change of the eigenvalues by the float32 rounding of T
+  // (|d|, |e| <= tnorm: 3 2^-24 tnorm) and the backward error of the float32
+  // counts (a few 2^-24 (|d| + |x|)); 2^-20 (tnorm + span) covers both
+  const double dp = 0x1p-20 * (tnorm + span);
   for (int k = tm.stid; k < n; k += tm.nthr) {
     // --- float32 bisection: count(lo) <= k < count(hi) ---
     float lo = (float)glo, hi = (float)ghi;
     for (int it = 0; it < 60; ++it) {
       const float mid = 0.5f * (lo + hi);
       if (mid <= lo || mid >= hi) break;
-      if (sturm_count_f32(n, df, e2f, mid, tinyf) <= k) lo = mid; else hi = mid;
+      if (sturm_count_f32(n, df, e2f, mid) <= k) lo = mid; else hi = mid;
     }
     const double w32 = fmax((double)hi - (double)lo, 4e-7 * tnorm + 1e-12);
     const double x0 = 0.5 * ((double)lo + (double)hi);
-    // --- float64 bracket [l, h) with count(l) <= k < count(h) ---
-    double l = x0 - 4.0 * w32, h = x0 + 4.0 * w32;
-    int cl = sturm_count_f64(n, d, e2, l), ch = sturm_count_f64(n, d, e2, h);
-    if (!(cl <= k && k < ch)) {
-      l = glo;
-      h = ghi;
-      cl = 0;
-      ch = n;
+    double l, h;
+    int cl, ch;
+    // --- isolation by float32 counts: the k-th eigenvalue of T lies within
+    // R = w32 + dp of x0, and if the float32 counts at x0 -+ 2R are k and
+    // k + 1 no other eigenvalue of T comes closer than R (Weyl), so
+    // [x0 - R, x0 + R] brackets it alone without float64 counts ---
+    const double R = w32 + dp;
+    if (sturm_count_f32(n, df, e2f, (float)(x0 - 2.0 * R)) == k &&
+        sturm_count_f32(n, df, e2f, (float)(x0 + 2.0 * R)) == k + 1) {
+      l = x0 - R;
+      h = x0 + R;
+      cl = k;
+      ch = k + 1;
+    } else {
+      // --- float64 bracket [l, h) with count(l) <= k < count(h) ---
+      l = x0 - 4.0 * w32;
+      h = x0 + 4.0 * w32;
+      cl = sturm_count_f64(n, d, e2, l);
+      ch = sturm_count_f64(n, d, e2, h);
+      if (!(cl <= k && k < ch)) {
+        l = glo;
+        h = ghi;
+        cl = 0;
+        ch = n;
+      }
     }
     // --- bisect until the bracket holds the k-th eigenvalue alone ---
     for (int it = 0; it < 200 && !(cl == k && ch == k + 1); ++it) {
@@ -666,7 +755,11 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
       // recurrence (eps |T|); a step that would leave the bracket becomes a
       // bisection step, and then (or after slow steps) the count at the new
       // point shrinks the bracket
+      // a Newton step of size s after one of size s0 (quadratic convergence,
+      // error ~ K s^2 with K ~ s / s0^2) leaves an error of about s^3 / s0^2:
+      // below tol the next evaluation (~5 n float64 instructions) is skipped
       const double tol = 4.0 * kEps * fmax(tnorm, fabs(x));
+      double sprev = 0.0;
       for (int it = 0; it < 16; ++it) {
         double xn = x - charpoly_ratio(n, d, e2, x);
         const bool bis = !(xn > l && xn < h);
@@ -674,6 +767,8 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
         const double step = fabs(xn - x);
         x = xn;
         if (!bis && step <= tol) break;
+        if (!bis && sprev > 0.0 && step <= 0.01 * sprev && step * step * step <= tol * sprev * sprev) break;
+        sprev = bis ? 0.0 : step;
         if (bis || it >= 3) {
           if (sturm_count_f64(n, d, e2, x) <= k) l = x; else h = x;
           if (h - l <= tol) break;
@@ -718,26 +813,38 @@ __device__ void team_rank_sort(Team<CL> &tm, int n, const double *in, double *ou
   tm.sync();
 }
 
+// Deterministic pseudo-random start in [1, 2) (any vector with a component
+// along the eigenvector works), assembled from the bits of a hash: no
+// float64 instruction.
 __device__ __forceinline__ double start_vector(int i, int j) {
-  // deterministic pseudo-random start in [0.5, 1.5) (any vector with a
-  // component along the eigenvector works)
   uint32_t h = 2654435761u * (uint32_t)(i + 1) ^ 40503u * (uint32_t)(j + 7);
   h ^= h >> 13;
   h *= 0x5bd1e995u;
   h ^= h >> 15;
-  return 0.5 + (double)(h & 0xffffff) / 16777216.0;
+  return __longlong_as_double((long long)(0x3ff0000000000000ull | ((uint64_t)h << 20)));
+}
+
+// |a| >= |b| for finite doubles, on the bit patterns (integer compare).
+__device__ __forceinline__ bool abs_ge(double a, double b) {
+  return (__double_as_longlong(a) & 0x7fffffffffffffffll) >= (__double_as_longlong(b) & 0x7fffffffffffffffll);
 }
 
 // Eigenvectors of the symmetric tridiagonal (d, e) for the m lowest
 // (sorted) eigenvalues lam[0..m) by inverse iteration with a partially
-// pivoted LU of T - lam I (the scheme of LAPACK's dstein: three solves,
-// re-orthogonalisation against the previous members of the cluster).
+// pivoted LU of T - lam I (the scheme of LAPACK's dstein: two solves, three
+// with re-orthogonalisation against the previous members of the cluster).
 // Clusters are runs of eigenvalues closer than ctol; each cluster is one
-// thread's work (over the team). d, e, lam: shared copies. Y: n x m
-// row-major global (column j = vector j). lu: global scratch of
-// 5 * n * nslot doubles; team threads [0, nslot) factorise (nslot <= team
-// threads). cl: global int [m + 1]; the lead CTA lists the clusters, the
-// count goes through gctl[2].
+// thread's work (over the team). A warp issues one float64 instruction per
+// ~64 cycles whatever its active lanes, so this serial per-thread work is
+// written for few float64 instructions per row: pivots by integer compares,
+// no branches (selects), reciprocals of the pivots by rcp_nr (stored, so
+// the solves multiply), start vectors from integer bits, and no scaling
+// between the solves (the growth stays far inside the float64 range: at
+// most (n / tiny)^3); one normalisation at the end.
+// d, e, lam: shared copies. Y: n x m row-major global (column j = vector
+// j). lu: global scratch of 5 * n * nslot doubles; team threads [0, nslot)
+// factorise (nslot <= team threads). cl: global int [m + 1]; the lead CTA
+// lists the clusters, the count goes through gctl[2].
 template <bool CL>
 __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const double *e,
                                  const double *lam, int m, double tnorm, double *Y, double *lu,
@@ -765,37 +872,29 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
     for (int j = j0; j < j1; ++j) {
       // separate exactly coincident shifts inside a cluster (dstein)
       const double lmb = lam[j] + (j - j0) * 10.0 * tiny;
-      // LU with partial pivoting of T - lmb I; rows hold (diag, super, super2)
+      // LU with partial pivoting of T - lmb I; rows hold (1/diag, super, super2).
+      // Pivots below tiny in magnitude are replaced by +-tiny (sign kept).
       double a = d[0] - lmb, bsup = n > 1 ? e[0] : 0.0;
       for (int i = 0; i < n - 1; ++i) {
         const double low = e[i];
         const double dn = d[i + 1] - lmb, en = (i + 1 < n - 1) ? e[i + 1] : 0.0;
-        if (fabs(a) >= fabs(low)) {
-          const double piv = a == 0.0 ? tiny : a;
-          const double mult = low / piv;
-          LU(U0, i) = piv;
-          LU(U1, i) = bsup;
-          LU(U2, i) = 0.0;
-          LU(Lm, i) = mult;
-          LU(Pv, i) = 0.0;
-          a = dn - mult * bsup;
-          bsup = en;
-        } else {
-          const double mult = a / low;
-          LU(U0, i) = low;
-          LU(U1, i) = dn;
-          LU(U2, i) = en;
-          LU(Lm, i) = mult;
-          LU(Pv, i) = 1.0;
-          a = bsup - mult * dn;
-          bsup = -mult * en;
-        }
+        const bool swap = !abs_ge(a, low);
+        double piv = swap ? low : a;
+        if (!abs_ge(piv, tiny)) piv = is_neg(piv) ? -tiny : tiny;
+        const double r = rcp_nr(piv);
+        const double mult = (swap ? a : low) * r;
+        LU(U0, i) = r;
+        LU(U1, i) = swap ? dn : bsup;
+        LU(U2, i) = swap ? en : 0.0;
+        LU(Lm, i) = mult;
+        LU(Pv, i) = swap ? 1.0 : 0.0;
+        a = fma(-mult, swap ? dn : bsup, swap ? bsup : dn);
+        bsup = swap ? flip_sign(mult) * en : en;
       }
-      LU(U0, n - 1) = a;
-      // tiny pivots perturbed (sign kept); U0 then holds the reciprocals
-      for (int i = 0; i < n; ++i) {
-        const double u = LU(U0, i);
-        LU(U0, i) = 1.0 / (fabs(u) < tiny ? copysign(tiny, u == 0.0 ? 1.0 : u) : u);
+      {
+        double piv = a;
+        if (!abs_ge(piv, tiny)) piv = is_neg(piv) ? -tiny : tiny;
+        LU(U0, n - 1) = rcp_nr(piv);
       }
       for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
       const int nsolve = (j1 - j0 > 1) ? 3 : 2;
@@ -805,36 +904,40 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         double carry = Y[j];
 #pragma unroll 4
         for (int i = 0; i < n - 1; ++i) {
-          double xi = carry, xn = Y[(size_t)(i + 1) * m + j];
-          if (LU(Pv, i) != 0.0) {
-            const double t = xi;
-            xi = xn;
-            xn = t;
-          }
+          const double yn = Y[(size_t)(i + 1) * m + j];
+          const bool sw = LU(Pv, i) != 0.0;
+          const double xi = sw ? yn : carry, xn = sw ? carry : yn;
           Y[(size_t)i * m + j] = xi;
-          carry = xn - LU(Lm, i) * xi;
+          carry = fma(-LU(Lm, i), xi, xn);
         }
         Y[(size_t)(n - 1) * m + j] = carry;
         // back substitution with the upper factor (two super-diagonals)
         double x1 = 0.0, x2 = 0.0;
 #pragma unroll 4
         for (int i = n - 1; i >= 0; --i) {
-          const double v = (Y[(size_t)i * m + j] - LU(U1, i) * x1 - LU(U2, i) * x2) * LU(U0, i);
+          const double v = fma(-LU(U2, i), x2, fma(-LU(U1, i), x1, Y[(size_t)i * m + j])) * LU(U0, i);
           Y[(size_t)i * m + j] = v;
           x2 = x1;
           x1 = v;
         }
-        // Gram-Schmidt against the earlier members of the cluster
+        // Gram-Schmidt against the earlier (normalised) members of the cluster
         for (int k = j0; k < j; ++k) {
           double dot = 0.0;
-          for (int i = 0; i < n; ++i) dot += Y[(size_t)i * m + k] * Y[(size_t)i * m + j];
-          for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] -= dot * Y[(size_t)i * m + k];
+          for (int i = 0; i < n; ++i) dot = fma(Y[(size_t)i * m + k], Y[(size_t)i * m + j], dot);
+          for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = fma(-dot, Y[(size_t)i * m + k], Y[(size_t)i * m + j]);
         }
-        double nrm = 0.0;
-        for (int i = 0; i < n; ++i) nrm += Y[(size_t)i * m + j] * Y[(size_t)i * m + j];
-        const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
-        for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+        if (j > j0 && it + 1 < nsolve) {
+          // keep the re-orthogonalised vector at unit scale for the next solve
+          double nrm = 0.0;
+          for (int i = 0; i < n; ++i) nrm = fma(Y[(size_t)i * m + j], Y[(size_t)i * m + j], nrm);
+          const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
+          for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+        }
       }
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm = fma(Y[(size_t)i * m + j], Y[(size_t)i * m + j], nrm);
+      const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
+      for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
     }
   }
 #undef LU

@@ -860,11 +860,13 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     attr = true;
   }
   // shared memory of class c: the base plus the rows of the Householder
-  // reduction of its largest possible molecule, when they fit
+  // reduction of its largest possible molecule (and, for clusters, one
+  // broadcast row), when they fit
   auto class_smem = [&](int c) -> size_t {
     const int csize = c >= 2 ? 1 << (c - 1) : 1;
     const int nub = (c + 1 < kClasses && a.thr[c + 1] != INT32_MAX) ? min(nmax, a.thr[c + 1] - 1) : nmax;
-    const size_t full = smem + (size_t)((nub + csize - 1) / csize) * nub * sizeof(double);
+    const int rows = (nub + csize - 1) / csize + (c >= 2 ? 1 : 0);
+    const size_t full = smem + (size_t)rows * nub * sizeof(double);
     return full <= (size_t)kMaxDynSmem ? full : smem;
   };
   // largest classes first: clusters, then one-SM CTAs, then the shared SMs
