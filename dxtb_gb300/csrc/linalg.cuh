@@ -9,8 +9,9 @@
 //     of the trailing matrix, two team barriers per reflector)
 //   -> eigenvalues: float32 bisection + float64 Newton, one thread each
 //      (team_tri_eigenvalues)
-//   -> eigenvectors of the lowest m eigenvalues only, by inverse iteration
-//      with a pivoted tridiagonal LU, one thread per eigenvalue cluster,
+//   -> eigenvectors of the lowest m eigenvalues only, one thread per
+//      eigenvalue cluster: the twisted factorisation for an isolated
+//      eigenvalue, inverse iteration with a pivoted tridiagonal LU and
 //      Gram-Schmidt inside clusters (team_tri_vectors)
 //   -> back-transformation of those m vectors, each CTA a block of
 //      vectors (team_back_transform: no team barrier per reflector).
@@ -113,19 +114,23 @@ __device__ void team_gemm(Team<CL> &tm, int M, int N, int K, double alpha, const
   // the diagonal only (M == N).
   const bool col_slow = (krange == kBLowerT || krange == kBUpper);
   const int ntile = lower_only ? tmm * (tmm + 1) / 2 : tmm * tnn;
-  for (int t = tm.tid; t < ntile; t += tm.nthr) {
+  // consecutive tiles go to different CTAs (stid), so that a cluster's CTAs
+  // share the long and the short k-ranges evenly; the triangle indices come
+  // from a float32 square root with integer corrections (a float64 square
+  // root costs a warp ~700 cycles on this part)
+  for (int t = tm.stid; t < ntile; t += tm.nthr) {
     int ti, tj;
     if (lower_only) {
       if (col_slow) {
         // column-major over the lower triangle: column tj holds tmm - tj tiles
         const int u = ntile - 1 - t;  // reverse: count from the short last columns
-        int c = (int)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+        int c = (int)((sqrtf(8.0f * (float)u + 1.0f) - 1.0f) * 0.5f);
         while ((c + 1) * (c + 2) / 2 <= u) ++c;
         while (c * (c + 1) / 2 > u) --c;
         tj = tmm - 1 - c;
         ti = tmm - 1 - (u - c * (c + 1) / 2);
       } else {
-        int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        int r = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
         while ((r + 1) * (r + 2) / 2 <= t) ++r;
         while (r * (r + 1) / 2 > t) --r;
         ti = r;
@@ -558,19 +563,18 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
 
 // Number of eigenvalues of the tridiagonal below x, in float32 and without
 // divisions: sign changes of the leading principal minors p_k of T - x I
-// (three-term recurrence p_{k+1} = (d_k - x) p_k - e2_{k-1} p_{k-1}, e2 = e^2).
-// A zero minor is replaced by a tiny value of the opposite sign of its
-// predecessor (it counts as a change, like a zero pivot replaced by -tiny).
+// (three-term recurrence p_{k+1} = (d_k - x) p_k - e2_{k-1} p_{k-1}, e2 = e^2),
+// read from the sign bits. An exact zero minor needs no fix-up: the next
+// minor is -e2 p_{k-1}, of the sign opposite to p_{k-1}, so a zero of
+// either sign adds exactly one change (a zero pivot counted as negative).
 // Every fourth row the pair is rescaled by 2^-+64 when the larger magnitude
-// leaves [2^-40, 2^40]. Everything is selects and sign-bit arithmetic: a
-// data-dependent branch per row made the count seven times slower.
+// leaves [2^-40, 2^40]. No data-dependent branch: the serial chain is one
+// float32 FMA per row (a branch per row made the count seven times slower).
 __device__ __forceinline__ int sturm_count_f32(int n, const float *d, const float *e2, float x) {
   float p0 = 1.0f, p1 = d[0] - x;
-  p1 = p1 == 0.0f ? -1e-30f : p1;
   int cnt = __float_as_int(p1) < 0 ? 1 : 0;
   auto step = [&](float dx, float ee) {
-    float p2 = fmaf(dx, p1, -ee * p0);
-    p2 = p2 == 0.0f ? (__float_as_int(p1) < 0 ? 1e-30f : -1e-30f) : p2;
+    const float p2 = fmaf(dx, p1, -ee * p0);
     cnt += (__float_as_int(p2) ^ __float_as_int(p1)) < 0 ? 1 : 0;
     p0 = p1;
     p1 = p2;
@@ -829,28 +833,186 @@ __device__ __forceinline__ bool abs_ge(double a, double b) {
   return (__double_as_longlong(a) & 0x7fffffffffffffffll) >= (__double_as_longlong(b) & 0x7fffffffffffffffll);
 }
 
+// Eigenvector of an isolated eigenvalue lmb of the tridiagonal (d, e;
+// e2 = e^2) by the twisted factorisation of T - lmb I (the vector of one
+// optimal inverse-iteration step, as in the MRRR "getvec" step), written
+// through the leading minors P[k] = det(T - lmb I)[0:k, 0:k] and trailing
+// minors Q[k] = det(T - lmb I)[k:n, k:n] so that no row needs a division:
+// the twist index r maximises |P[r] Q[r+1]| (the diagonal of the adjugate,
+// proportional to z_r^2), and with z_r = 1
+//   z_i = P[i] / P[r] prod_{t=i}^{r-1} (-e_t)          (i < r)
+//   z_i = Q[i+1] / Q[r+1] prod_{t=r}^{i-1} (-e_t)      (i > r).
+// Both minor sequences are three-term FMA recurrences; they and the running
+// products are rescaled by 2^-+400 when they leave [2^-400, 2^400]
+// (exponent test on the bits, every fourth row), with the scale counts kept per row
+// (as bit patterns in the scratch columns SP, SQ), so no product of two kept
+// values overflows; components below 2^-800 of z_r are set to zero. About
+// eleven float64 instructions per row in all, against ~20 and four
+// memory-bound sweeps of the pivoted LU with two solves. P, Q, SP, SQ: per-thread scratch columns of n doubles (stride
+// nslot, column tid). Writes the normalised vector to column j of Y (n x m).
+__device__ __forceinline__ void tri_vector_twisted(int n, const double *d, const double *e,
+                                                   const double *e2, double lmb, double *__restrict__ Y,
+                                                   int m, int j, double *__restrict__ P,
+                                                   double *__restrict__ Q, double *__restrict__ SP,
+                                                   double *__restrict__ SQ, int nslot, int tid) {
+#define AT(arr, i) arr[(size_t)(i) * nslot + tid]
+  auto expo = [](double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7ff); };
+  auto keep = [&](double &a, double &b, int &cnt) {
+    const int em = max(expo(a), expo(b));
+    if (em > 1023 + 400 || em < 1023 - 400) {
+      const bool big = em > 1023;
+      const double sc = big ? 0x1p-400 : 0x1p400;
+      a *= sc;
+      b *= sc;
+      cnt += big ? 1 : -1;
+    }
+  };
+  auto cbits = [](int c) { return __longlong_as_double((long long)c); };
+  auto cint = [](double v) { return (int)__double_as_longlong(v); };
+  // Rows go in blocks of four: the block's loads are issued first and the
+  // range test (a branch) runs once per block. Four rows of growth
+  // (|minor ratio| <= 2 |T| + |T|^2, |e| <= |T|) stay inside the float64 range
+  // for |T| < 2^16, which the caller checks
+  // forward: P[k] (k = 0 .. n-1) at slot k
+  {
+    double pk = 1.0, pkm = 0.0;
+    int cnt = 0;
+    for (int k0 = 0; k0 < n; k0 += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + u;
+        if (k < n) {
+          AT(P, k) = pk;
+          AT(SP, k) = cbits(cnt);
+          const double ee = k > 0 ? e2[k - 1] : 0.0;
+          const double pn = fma(d[k] - lmb, pk, -ee * pkm);
+          pkm = pk;
+          pk = pn;
+        }
+      }
+      keep(pk, pkm, cnt);
+    }
+  }
+  // backward: Q[k + 1] at slot k (k = n-1 .. 0); the twist index on the way
+  int r = n - 1;
+  {
+    double q1 = 1.0, q2 = 0.0;  // Q[k+1], Q[k+2]
+    int cnt = 0, best = INT_MIN;
+    for (int k0 = n - 1; k0 >= 0; k0 -= 4) {
+      double pv[4], sv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 - u;
+        pv[u] = k >= 0 ? AT(P, k) : 0.0;
+        sv[u] = k >= 0 ? AT(SP, k) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 - u;
+        if (k >= 0) {
+          AT(Q, k) = q1;
+          AT(SQ, k) = cbits(cnt);
+          // log2 |P[k] Q[k+1]| up to the mantissas (a zero minor counts as tiny)
+          const int mag = expo(pv[u]) + expo(q1) + 400 * (cint(sv[u]) + cnt);
+          if (mag > best) {
+            best = mag;
+            r = k;
+          }
+          const double ee = k < n - 1 ? e2[k] : 0.0;
+          const double qn = fma(d[k] - lmb, q1, -ee * q2);
+          q2 = q1;
+          q1 = qn;
+        }
+      }
+      keep(q1, q2, cnt);
+    }
+  }
+  // the vector from the twist outwards
+  auto factor = [](int c) {
+    return c < -2 ? 0.0 : (c == -2 ? 0x1p-800 : (c == -1 ? 0x1p-400 : (c == 0 ? 1.0 : (c == 1 ? 0x1p400 : 0x1p800))));
+  };
+  double nrm = 1.0;
+  Y[(size_t)r * m + j] = 1.0;
+  {
+    double E = rcp_nr(AT(P, r)), one = 1.0;
+    int cnt = -cint(AT(SP, r));
+    for (int i0 = r - 1; i0 >= 0; i0 -= 4) {
+      double pv[4], sv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        pv[u] = i0 - u >= 0 ? AT(P, i0 - u) : 0.0;
+        sv[u] = i0 - u >= 0 ? AT(SP, i0 - u) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 - u;
+        if (i >= 0) {
+          E *= -e[i];
+          const double z = (E * pv[u]) * factor(cnt + cint(sv[u]));
+          Y[(size_t)i * m + j] = z;
+          nrm = fma(z, z, nrm);
+        }
+      }
+      keep(E, one, cnt);
+    }
+  }
+  {
+    double E = rcp_nr(AT(Q, r)), one = 1.0;
+    int cnt = -cint(AT(SQ, r));
+    for (int i0 = r + 1; i0 < n; i0 += 4) {
+      double qv[4], sv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        qv[u] = i0 + u < n ? AT(Q, i0 + u) : 0.0;
+        sv[u] = i0 + u < n ? AT(SQ, i0 + u) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u;
+        if (i < n) {
+          E *= -e[i - 1];
+          const double z = (E * qv[u]) * factor(cnt + cint(sv[u]));
+          Y[(size_t)i * m + j] = z;
+          nrm = fma(z, z, nrm);
+        }
+      }
+      keep(E, one, cnt);
+    }
+  }
+  const double inv = 1.0 / sqrt(nrm);
+#pragma unroll 4
+  for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+#undef AT
+}
+
 // Eigenvectors of the symmetric tridiagonal (d, e) for the m lowest
-// (sorted) eigenvalues lam[0..m) by inverse iteration with a partially
-// pivoted LU of T - lam I (the scheme of LAPACK's dstein: two solves, three
-// with re-orthogonalisation against the previous members of the cluster).
-// Clusters are runs of eigenvalues closer than ctol; each cluster is one
-// thread's work (over the team). A warp issues one float64 instruction per
+// (sorted) eigenvalues lam[0..m). Clusters are runs of eigenvalues closer
+// than ctol; each cluster is one thread's work (over the team). An isolated
+// eigenvalue takes the twisted factorisation (tri_vector_twisted); the
+// members of a cluster take inverse iteration with a partially pivoted LU
+// of T - lam I (the scheme of LAPACK's dstein: three solves with
+// re-orthogonalisation against the previous members of the cluster). A warp issues one float64 instruction per
 // ~64 cycles whatever its active lanes, so this serial per-thread work is
 // written for few float64 instructions per row: pivots by integer compares,
 // no branches (selects), reciprocals of the pivots by rcp_nr (stored, so
 // the solves multiply), start vectors from integer bits, and no scaling
 // between the solves (the growth stays far inside the float64 range: at
 // most (n / tiny)^3); one normalisation at the end.
-// d, e, lam: shared copies. Y: n x m row-major global (column j = vector
-// j). lu: global scratch of 5 * n * nslot doubles; team threads [0, nslot)
-// factorise (nslot <= team threads). cl: global int [m + 1]; the lead CTA
-// lists the clusters, the count goes through gctl[2].
+// d, e, lam: shared copies; e2s: shared scratch of n doubles (e^2). Y: n x m
+// row-major global (column j = vector j). lu: global scratch of
+// 5 * n * nslot doubles; team threads [0, nslot) factorise (nslot <= team
+// threads). cl: global int [m + 1]; the lead CTA lists the clusters, the
+// count goes through gctl[2].
 template <bool CL>
 __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const double *e,
                                  const double *lam, int m, double tnorm, double *Y, double *lu,
-                                 int nslot, int *cl) {
+                                 int nslot, int *cl, double *e2s) {
   const double ctol = 1e-6 * fmax(tnorm, 1.0);
   const double tiny = kEps * fmax(tnorm, 1.0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) e2s[i] = i < n - 1 ? e[i] * e[i] : 0.0;
+  // the twisted vector's range bookkeeping (rescaling every fourth row)
+  // assumes |T| within 2^-+16 (a Fock matrix in Hartree: ~1..100)
+  const bool twist_ok = tnorm < 0x1p16 && tnorm > 0x1p-16;
   if (tm.lead() && threadIdx.x == 0) {
     int c = 0;
     cl[c++] = 0;
@@ -869,6 +1031,10 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
 #define LU(arr, i) arr[(size_t)(i) * nslot + tid]
   for (int c = tid; tid < nslot && c < ncl; c += nslot) {
     const int j0 = ldi<CL>(cl + c), j1 = ldi<CL>(cl + c + 1);
+    if (j1 - j0 == 1 && twist_ok) {
+      tri_vector_twisted(n, d, e, e2s, lam[j0], Y, m, j0, U0, U1, U2, Lm, nslot, tid);
+      continue;
+    }
     for (int j = j0; j < j1; ++j) {
       // separate exactly coincident shifts inside a cluster (dstein)
       const double lmb = lam[j] + (j - j0) * 10.0 * tiny;
@@ -979,7 +1145,7 @@ __device__ void team_back_transform(Team<CL> &tm, int n, const double *A, const 
         const int G = max(1, min(kPart / npair, (int)blockDim.x / npair));
         for (int q = threadIdx.x; q < G * npair; q += blockDim.x) {
           const int pr = q % npair, g = q / npair;
-          int j = (int)((sqrt(8.0 * (double)pr + 1.0) + 1.0) * 0.5);  // pr -> (i < j)
+          int j = (int)((sqrtf(8.0f * (float)pr + 1.0f) + 1.0f) * 0.5f);  // pr -> (i < j)
           while (j * (j - 1) / 2 > pr) --j;
           while ((j + 1) * j / 2 <= pr) ++j;
           const int i = pr - j * (j - 1) / 2;
@@ -989,7 +1155,7 @@ __device__ void team_back_transform(Team<CL> &tm, int n, const double *A, const 
         }
         __syncthreads();
         for (int pr = threadIdx.x; pr < npair; pr += blockDim.x) {
-          int j = (int)((sqrt(8.0 * (double)pr + 1.0) + 1.0) * 0.5);
+          int j = (int)((sqrtf(8.0f * (float)pr + 1.0f) + 1.0f) * 0.5f);
           while (j * (j - 1) / 2 > pr) --j;
           while ((j + 1) * j / 2 <= pr) ++j;
           const int i = pr - j * (j - 1) / 2;

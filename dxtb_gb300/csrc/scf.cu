@@ -547,7 +547,8 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm, bo
     }
     mo = ldi<CL>(tm.gctl + 1);
     // ---- eigenvectors of the mo lowest orbitals only ----
-    team_tri_vectors(tm, n, sd, se, sw, mo, tnorm, w.Zt, w.lu, (int)min((int64_t)tm.nthr, lu_slots(n)), w.cl);
+    team_tri_vectors(tm, n, sd, se, sw, mo, tnorm, w.Zt, w.lu, (int)min((int64_t)tm.nthr, lu_slots(n)), w.cl,
+                     reinterpret_cast<double *>(df));
     team_back_transform(tm, n, w.A, w.tau, w.Zt, mo, w.lu, spart);  // lu: free after the vectors
     // ---- C^T = Y^T X (orbital j is row j; X lower -> k >= i) ----
     team_gemm<true, false>(tm, mo, n, n, 1.0, w.Zt, mo, w.Linv, n, 0.0, C, n, kBUpper);
