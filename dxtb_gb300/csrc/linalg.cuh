@@ -522,13 +522,13 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
     }
     __syncthreads();
     // ---- D ----
-    // warp 0's serial chain keeps its sub-partition's float64 pipe to itself
-    // (warps 4, 8, 12 share it and stay idle; a shared pipe slowed the chain
-    // several fold); the update runs on the warps of the other three
+    // warp 0 runs the serial chain of the next scalars, the other warps the
+    // update (keeping the warps of warp 0's sub-partition idle shortened the
+    // chain but cost more update throughput than it saved: measured)
     if (ty == 0) {
       if (k + 1 < n - 2) scalars(k + 1, m - 1);
-    } else if ((ty & 3) != 0) {
-      const int nu = nty - ((nty + 3) >> 2), uw = ty - (ty >> 2) - 1;
+    } else {
+      const int nu = nty - 1, uw = ty - 1;
       for (int it = uw; it < mc * ncg; it += nu) {
         const int jj = it / ncg, c = (it % ncg) * 32 + tx, r = rb + C * jj;
         // row 0 of A22 leaves the trailing matrix: only its diagonal (d of

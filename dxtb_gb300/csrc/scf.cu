@@ -318,15 +318,24 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
     // v = Gm^T dx, c = dx - Gm dy, d = v / (dy . v)
     if (br.nrank >= kRank) br.nrank = 0;  // "restart" reduction of a full memory (not reached: kRank >= maxiter)
     const int nrank = br.nrank;
+    // dx and dy once (into the x_prev / F_prev slots, rewritten below): a
+    // float64 instruction costs a warp ~64 cycles, so the dot products below
+    // read them instead of forming the differences again per history vector
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      const double xt = w.x[t];
+      w.rold[t] = (xt - w.g[t]) - w.rold[t];
+      w.xold[t] = xt - w.xold[t];
+    }
+    __syncthreads();
     for (int k = wid; k < 2 * nrank; k += nw) {
       const int kk = k >> 1;
       double s = 0.0;
       if ((k & 1) == 0) {
         const double *ck = w.hx + (size_t)kk * N;
-        for (int t = lane; t < N; t += 32) s += ck[t] * (w.x[t] - w.xold[t]);
+        for (int t = lane; t < N; t += 32) s = fma(ck[t], w.xold[t], s);
       } else {
         const double *dk = w.hr + (size_t)kk * N;
-        for (int t = lane; t < N; t += 32) s += dk[t] * ((w.x[t] - w.g[t]) - w.rold[t]);
+        for (int t = lane; t < N; t += 32) s = fma(dk[t], w.rold[t], s);
       }
       s = warp_sum(s);
       if (lane == 0) {
@@ -337,8 +346,8 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
     double *cn = w.hx + (size_t)nrank * N, *dn = w.hr + (size_t)nrank * N;
     double pdv = 0.0;
     for (int t = threadIdx.x; t < N; t += blockDim.x) {
-      const double dxt = w.x[t] - w.xold[t];
-      const double dyt = (w.x[t] - w.g[t]) - w.rold[t];
+      const double dxt = w.xold[t];
+      const double dyt = w.rold[t];
       double v = 0.5 * dxt, gdy = 0.5 * dyt;
       for (int k = 0; k < nrank; ++k) {
         v += w.hr[(size_t)k * N + t] * sdot[k];
