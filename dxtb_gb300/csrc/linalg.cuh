@@ -799,20 +799,29 @@ __device__ void team_tri_eigenvalues(Team<CL> &tm, int n, const double *d, const
   tm.sync();
 }
 
-// Ascending sort by rank (ties broken by index): out[rank(i)] = in[i]; in
-// is copied to the shared scratch s (n doubles) first. out: global.
+// Ascending sort by rank (ties broken by index): out[rank(i)] = in[i]. The
+// values go to the shared scratch s (n doubles) as order-preserving int64
+// keys (negative numbers with the magnitude bits flipped, -0 as +0), so the
+// n^2 comparisons are integer ones instead of float64 (finite inputs).
+// out: global.
 template <bool CL>
 __device__ void team_rank_sort(Team<CL> &tm, int n, const double *in, double *out, double *s) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = ld<CL>(in + i);
+  auto key = [](double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b < 0 ? (b ^ 0x7fffffffffffffffll) : b;
+  };
+  long long *sk = reinterpret_cast<long long *>(s);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sk[i] = key(ld<CL>(in + i));
   __syncthreads();
   for (int i = tm.stid; i < n; i += tm.nthr) {
-    const double v = s[i];
+    const long long v = sk[i];
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      const double u = s[j];
+      const long long u = sk[j];
       r += (u < v) || (u == v && j < i);
     }
-    out[r] = v;
+    out[r] = __longlong_as_double(v < 0 ? (v ^ 0x7fffffffffffffffll) : v);
   }
   tm.sync();
 }

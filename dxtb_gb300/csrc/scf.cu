@@ -107,13 +107,23 @@ __device__ bool fermi_warp(int n, const double *eps, double nel, double kt, doub
   const int khomo = min(max((int)ceil(nel) - 1, 0), n - 1);
   double mu = 0.5 * (eps[khomo] + eps[min(khomo + 1, n - 1)]);
   const double ikt = 1.0 / kt;
+  // f(x) = 1 / (1 + e^x) from one exp(-|x|) and a reciprocal (rcp_nr: 1 + e
+  // lies in [1, 2]); beyond |x| = 40 f is 0 or 1 to 4e-18, below the
+  // electron-count threshold, and the exp is skipped (the eigenvalues are
+  // sorted, so whole warp iterations far from mu skip it together)
+  auto occ = [](double x) {
+    if (x > 40.0) return 0.0;
+    if (x < -40.0) return 1.0;
+    const double ex = exp(-fabs(x));
+    const double r = rcp_nr(1.0 + ex);
+    return x > 0.0 ? ex * r : r;
+  };
   for (int it = 0; it < 200; ++it) {
     double s = 0.0, ds = 0.0;
     for (int j = lane; j < n; j += 32) {
-      const double x = (eps[j] - mu) * ikt;
-      const double v = x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+      const double v = occ((eps[j] - mu) * ikt);
       s += v;
-      ds += v * (1.0 - v);
+      ds = fma(v, 1.0 - v, ds);
     }
     s = warp_sum(s) - nel;
     ds = warp_sum(ds) * ikt;
@@ -126,8 +136,7 @@ __device__ bool fermi_warp(int n, const double *eps, double nel, double kt, doub
   }
   double s = 0.0;
   for (int j = lane; j < n; j += 32) {
-    const double x = (eps[j] - mu) / kt;
-    const double v = x > 0.0 ? exp(-x) / (1.0 + exp(-x)) : 1.0 / (1.0 + exp(x));
+    const double v = occ((eps[j] - mu) * ikt);
     f[j] = v;
     s += v;
   }
