@@ -5,8 +5,10 @@
 // times; each ends with a team barrier unless stated otherwise.
 //
 // The symmetric eigenproblem of the SCF is solved as
-//   Householder tridiagonalisation  (team_tridiag: the CTAs share the rows
-//     of the trailing matrix, two team barriers per reflector)
+//   Householder tridiagonalisation  (team_tridiag: row i belongs to CTA
+//     i mod size and stays in its shared memory where it fits; only vectors
+//     move between the CTAs, through distributed shared memory; two team
+//     barriers per reflector)
 //   -> eigenvalues: float32 bisection + float64 Newton, one thread each
 //      (team_tri_eigenvalues)
 //   -> eigenvectors of the lowest m eigenvalues only, one thread per
@@ -20,7 +22,17 @@
 //
 // In a cluster team, data written by another CTA is read with ld.global.cg
 // (L2, never a stale L1 line) after a barrier.cluster arrive.release /
-// wait.acquire pair; a one-CTA team uses plain loads and __syncthreads.
+// wait.acquire pair, or from that CTA's shared memory (mapa +
+// ld/st.shared::cluster, team_tridiag); a one-CTA team uses plain loads and
+// __syncthreads.
+//
+// A float64 instruction costs a warp ~64 cycles on this part whatever its
+// active lanes (the SM issues about one warp-instruction per 19 cycles over
+// all warps), so the serial and per-thread parts are written for few
+// float64 instructions: float32 seeds refined by one Newton-Raphson step
+// instead of divisions and square roots, selects instead of per-row
+// branches, integer compares on the bit patterns, float32 wherever a
+// float64 step checks or refines the result.
 #pragma once
 #include "common.cuh"
 

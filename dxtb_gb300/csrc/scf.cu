@@ -38,7 +38,8 @@ struct MolView {
 };
 
 __host__ __device__ inline int64_t lu_slots(int64_t n) { return n < kLuSlots ? n : kLuSlots; }
-// inverse-iteration factors, reused afterwards by the blocked back-transform (16 n)
+// inverse-iteration factors or the minors of the twisted eigenvectors (5 n per
+// slot), reused afterwards by the blocked back-transform (16 n)
 __host__ __device__ inline int64_t lu_size(int64_t n) {
   const int64_t a = 5 * n * lu_slots(n), b = 16 * n;
   return a > b ? a : b;
