@@ -198,14 +198,16 @@ int32_t dxtb_multipole_raw(const dxtb_batch *b, const double *par_f,
  * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
 int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
 
-/* Self-consistent field for every molecule of the batch in one persistent
- * launch, one CTA per molecule (scf/iterator.py:51-144 with scf/pure/*,
+/* Self-consistent field for every molecule of the batch, one persistent
+ * launch per size class and one team per molecule (a CTA, or a thread-block
+ * cluster for the larger classes) (scf/iterator.py:51-144 with scf/pure/*,
  * wavefunction/filling.py:428-742, exlibs/xitorch symeig): Fock build,
  * generalized eigensolve, Fermi occupations at kT, density, Mulliken
  * charges and multipole moments, potentials, and the limited-memory
  * Broyden root solve of x - G(x) on the potential (xitorch broyden1,
  * exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265); per-molecule
- * convergence |dx|_2 < tol and |x - G(x)|_2 < tol, iteration cap. order: [nmol] launch order (largest first) or null. Inputs are the
+ * convergence |dx|_2 < tol and |x - G(x)|_2 < tol, iteration cap.
+ * order: [nmol] launch order (largest first) or null. Inputs are the
  * integrals and caches of the calls above, n0 [naos] reference occupation,
  * nel [nmol][2] alpha/beta electrons, gb_mat [nat2] or null. Outputs:
  * density [mat], wdensity [mat] (energy-weighted, may be null), coeff [mat]
