@@ -448,7 +448,7 @@ __global__ void k_grad_mol(dxtb_batch b, const double *__restrict__ pf_,
         const double df3M = -f3 * f3 * 6.0 * dmp3 * r3d / M, df5M = -f5 * f5 * 6.0 * dmp5 * r5d / M;
         const double iR = 1.0 / R, iR3 = iR * iR * iR, iR5 = iR3 * iR * iR;
         const double h3 = iR3 * f3, dh3 = -3.0 * iR3 * iR * f3 + iR3 * df3;
-        const double k3 = iR3 * f5, dk3 = -3.0 * iR3 * iR * f5 + iR3 * df5;
+        const double dk3 = -3.0 * iR3 * iR * f5 + iR3 * df5;  // d/dR of k3 = f5 / R^3
         const double k5 = iR5 * f5, dk5 = -5.0 * iR5 * iR * f5 + iR5 * df5;
         double gr[3] = {0.0, 0.0, 0.0};
         double dM = 0.0;

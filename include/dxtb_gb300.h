@@ -40,7 +40,7 @@ extern "C" {
 
 /* ---- parameter tables ---------------------------------------------------
  * Flat float64 / int32 arrays filled by the host from the GFN parameter
- * files (param/gfn{1,2}/*.toml). A "shell type" is one shell of one
+ * files (the TOML tables under param/gfn{1,2}). A "shell type" is one shell of one
  * element; element Z owns shell types [EL_SH0[Z], EL_SH0[Z] + EL_NSH[Z]).
  */
 #define DXTB_MAXZ 87
@@ -200,7 +200,7 @@ int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
 
 /* Self-consistent field for every molecule of the batch, one persistent
  * launch per size class and one team per molecule (a CTA, or a thread-block
- * cluster for the larger classes) (scf/iterator.py:51-144 with scf/pure/*,
+ * cluster for the larger classes) (scf/iterator.py:51-144 with the scf/pure modules,
  * wavefunction/filling.py:428-742, exlibs/xitorch symeig): Fock build,
  * generalized eigensolve, Fermi occupations at kT, density, Mulliken
  * charges and multipole moments, potentials, and the limited-memory
