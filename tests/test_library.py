@@ -83,3 +83,42 @@ def test_workloads_deterministic_and_valid():
         assert d.min() >= 2.0 - 1e-12
     (num, pos), = config_molecules(1)
     assert sorted(num.tolist()).count(1) == 12 and len(num) == 24
+
+
+def test_size_class_policy_host_calls():
+    """The size-class thresholds are host state: defaults, validation and
+    restore work without a GPU (no CUDA call is made)."""
+    import ctypes as C
+
+    from dxtb_gb300 import build
+
+    L = C.CDLL(str(build.build()))
+    L.dxtb_scf_get_size_classes.restype = C.c_int32
+    L.dxtb_scf_set_size_classes.restype = C.c_int32
+    cur = (C.c_int32 * 5)()
+    assert L.dxtb_scf_get_size_classes(cur) == 0
+    saved = list(cur)
+    assert saved == sorted(saved) and saved[0] >= 1
+    try:
+        assert L.dxtb_scf_set_size_classes((C.c_int32 * 5)(100, 90, 200, 300, 400)) == 1  # decreasing
+        assert L.dxtb_scf_set_size_classes((C.c_int32 * 5)(0, 90, 200, 300, 400)) == 1  # below 1
+        assert L.dxtb_scf_set_size_classes((C.c_int32 * 5)(64, 96, 128, 256, 512)) == 0
+        got = (C.c_int32 * 5)()
+        assert L.dxtb_scf_get_size_classes(got) == 0
+        assert list(got) == [64, 96, 128, 256, 512]
+    finally:
+        assert L.dxtb_scf_set_size_classes((C.c_int32 * 5)(*saved)) == 0
+
+
+def test_scf_workspace_grows_with_size():
+    import ctypes as C
+
+    from dxtb_gb300 import build
+
+    L = C.CDLL(str(build.build()))
+    L.dxtb_scf_workspace_mol.restype = C.c_int64
+    L.dxtb_scf_workspace_mol.argtypes = [C.c_int64, C.c_int64]
+    a, b = L.dxtb_scf_workspace_mol(90, 30), L.dxtb_scf_workspace_mol(172, 60)
+    assert 0 < a < b
+    # at least the three n x n matrices of the molecule
+    assert a >= 3 * 90 * 90 and b >= 3 * 172 * 172
