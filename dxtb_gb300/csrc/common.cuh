@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/dxtb_gb300.h"
 
 #define DXTB_CHECK_LAUNCH()                                   \
@@ -88,9 +90,11 @@ __device__ __forceinline__ bool in_class(const ClassFilter &f, const dxtb_batch 
 
 // SM count of the current device, cached per device (host side).
 inline int32_t device_sms(int *sms) {
+  static std::mutex mu;
   static int cache[64] = {0};
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(mu);
   if (cache[dev] == 0) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
@@ -98,6 +102,28 @@ inline int32_t device_sms(int *sms) {
     cache[dev] = v;
   }
   *sms = cache[dev];
+  return DXTB_OK;
+}
+
+// One-time set-up per device (host side). CUDA keeps kernel attributes such
+// as the dynamic shared-memory limit per device, so each device runs `setup`
+// on its first use; `setup` returns false on a CUDA error, and the next call
+// on that device tries again.
+struct PerDeviceOnce {
+  std::mutex mu;
+  bool done[64] = {};
+};
+template <class F>
+inline int32_t per_device_once(PerDeviceOnce &once, F &&setup) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DXTB_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(once.mu);
+  if (once.done[dev]) return DXTB_OK;
+  if (!setup()) {
+    cudaGetLastError();
+    return DXTB_ERR_LAUNCH;
+  }
+  once.done[dev] = true;
   return DXTB_OK;
 }
 

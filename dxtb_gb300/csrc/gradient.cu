@@ -553,11 +553,12 @@ int32_t launch_gradient(const dxtb_batch *b, const double *par_f, const int32_t 
   // The multipole (GFN2) terms are taken iff the dipole integrals are given.
   const int multipole = dipole != nullptr;
   if (multipole && (!vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_grad_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gSmem);
-    attr = true;
-  }
+  static PerDeviceOnce attr;
+  if (per_device_once(attr, [] {
+        return cudaFuncSetAttribute(k_grad_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)gSmem) == cudaSuccess;
+      }) != DXTB_OK)
+    return DXTB_ERR_LAUNCH;
   const int64_t bound = (int64_t)b->nmol * b->max_nsh * (b->max_nsh + 1) / 2;
   if (bound > 0) {
     int sms = 0;
@@ -570,7 +571,9 @@ int32_t launch_gradient(const dxtb_batch *b, const double *par_f, const int32_t 
   }
   const size_t smem = sizeof(double) * (size_t)(b->max_nsh + 3 * b->max_nat + 8);
   if (smem > 200 * 1024) return DXTB_ERR_TOO_LARGE;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_grad_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_grad_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DXTB_ERR_LAUNCH;
   k_grad_mol<<<b->nmol, 128, smem, st>>>(*b, par_f, par_i, cn, mrad, q, dp, qp, multipole, dedcn, grad, f);
   DXTB_CHECK_LAUNCH();
   return DXTB_OK;

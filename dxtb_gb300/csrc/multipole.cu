@@ -335,12 +335,14 @@ static int32_t launch_multipole(const dxtb_batch *b, const double *par_f, const 
   int sms = 0;
   if (device_sms(&sms) != DXTB_OK) return DXTB_ERR_LAUNCH;
   const int64_t blocks = min((bound + kWarps - 1) / kWarps, (int64_t)sms * 2 * 8);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_multipole<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
-    cudaFuncSetAttribute(k_multipole<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
-    attr_set = true;
-  }
+  static PerDeviceOnce attr;
+  if (per_device_once(attr, [] {
+        return cudaFuncSetAttribute(k_multipole<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmem) == cudaSuccess &&
+               cudaFuncSetAttribute(k_multipole<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmem) == cudaSuccess;
+      }) != DXTB_OK)
+    return DXTB_ERR_LAUNCH;
   if (mode == 0)
     k_multipole<0><<<(unsigned)blocks, kWarps * 32, kSmem, st>>>(*b, par_f, par_i, cn, ncomp, S, H, D, Q);
   else

@@ -784,16 +784,19 @@ static int32_t side_stream(cudaStream_t caller, SideStream **out) {
   return DXTB_OK;
 }
 
-// Largest usable cluster size of k_scf_cluster with `smem` bytes of dynamic
-// shared memory (cached per device and shared-memory size).
-static int cluster_cap(size_t smem) {
+// Largest usable cluster size of k_scf_cluster (cached per device). The
+// occupancy query uses the largest dynamic shared memory any cluster launch
+// asks for (kMaxDynSmem): a size placeable there is placeable at every
+// smaller launch size, so no class launch is judged placeable at a smaller
+// size than it uses.
+static int cluster_cap() {
   static std::mutex mu;
   static int cap_dev[64] = {0};
-  static size_t cap_smem[64] = {0};
+  const size_t smem = kMaxDynSmem;
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
   std::lock_guard<std::mutex> lock(mu);
-  if (cap_dev[dev] != 0 && cap_smem[dev] >= smem) return cap_dev[dev];
+  if (cap_dev[dev] != 0) return cap_dev[dev];
   if (cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
       cudaFuncSetAttribute(k_scf_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem) !=
           cudaSuccess) {
@@ -821,7 +824,6 @@ static int cluster_cap(size_t smem) {
     cap = c;
   }
   cap_dev[dev] = cap;
-  cap_smem[dev] = smem;
   return cap;
 }
 
@@ -854,7 +856,7 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
   // clusters need the launch order; classes beyond the cluster cap fold down
   int top = a.order ? 5 : 1;
   if (top > 1 && scf_class(a.thr, nmax) >= 2) {
-    const int cap = cluster_cap(smem);
+    const int cap = cluster_cap();
     int c = 1;
     while ((2 << (c - 1)) <= cap && c < 5) ++c;  // largest class whose cluster fits
     top = cap >= 2 ? c : 1;
@@ -873,12 +875,15 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     for (int c = 0; c <= cmax; ++c)
       if (cudaStreamWaitEvent(ss->s[c], ss->fork, 0) != cudaSuccess) return DXTB_ERR_LAUNCH;
   }
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_scf<kScfThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
-    cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
-    attr = true;
-  }
+  static PerDeviceOnce attr;
+  if (per_device_once(attr, [] {
+        return cudaFuncSetAttribute(k_scf<kScfThreads, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMaxDynSmem) == cudaSuccess &&
+               cudaFuncSetAttribute(k_scf<kScfBigThreads, 1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kMaxDynSmem) == cudaSuccess;
+      }) != DXTB_OK)
+    return DXTB_ERR_LAUNCH;
   // shared memory of class c: the base plus the rows of the Householder
   // reduction of its largest possible molecule (and, for clusters, one
   // broadcast row), when they fit
@@ -1059,17 +1064,18 @@ extern "C" int32_t dxtb_scf_gradient(
 // ---------------------------------------------------------------------------
 // SCF entry point for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc at all: code that runs while a CUDA
-// graph is being captured by someone else, hosts that hand the library a
-// fixed memory pool and forbid further device allocations, or plugin hosts
-// whose allocator is not reachable from the C ABI. dxtb_scf_noalloc serves
-// them: it runs the same persistent SCF kernel as dxtb_scf, but its scratch
-// workspace is a fixed array in the library's own device memory, so the
-// caller passes only the inputs and the output buffers.
+// Some callers must not call cudaMalloc: hosts that hand the library a fixed
+// device-memory pool and forbid allocations outside it, or plugin hosts whose
+// allocator is not reachable from the C ABI. dxtb_scf_noalloc serves them: it
+// runs the same persistent SCF kernels as dxtb_scf, but its scratch workspace
+// is a fixed array in the library's own device memory, so the caller passes
+// only the inputs and the output buffers.
 //
 // The array holds DXTB_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) and every
 // GPU that loads the library keeps it until the process exits. Batches whose
-// workspace does not fit are rejected with DXTB_ERR_TOO_LARGE.
+// workspace does not fit are rejected with DXTB_ERR_TOO_LARGE. The size is
+// computed on the device from the batch's offset tables and read back once
+// per call (one synchronisation of the caller's stream).
 // ---------------------------------------------------------------------------
 #include <mutex>
 
@@ -1124,7 +1130,7 @@ extern "C" int32_t dxtb_scf_noalloc(
     double *evals, double *occ, double *q, double *dp, double *qp, double *vorb, double *vdp,
     double *vqp, double *energies, int32_t *status, void *stream) {
   if (!b || b->nmol <= 0) return DXTB_ERR_ARGS;
-  // header (nmol + 2 int64) must fit before the workspace
+  // the header (nmol + 2 int64, rounded up to 32 words) precedes the workspace
   const int64_t ws_start = ((kNoallocHeader + b->nmol + 1) + 31) / 32 * 32;
   if (ws_start >= DXTB_NOALLOC_SCRATCH_DOUBLES) return DXTB_ERR_TOO_LARGE;
   double *scratch = nullptr;

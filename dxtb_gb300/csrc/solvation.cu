@@ -304,8 +304,9 @@ extern "C" int32_t dxtb_born_matrix(const dxtb_batch *b, const double *par_f, co
   const size_t smem = sizeof(double) * 5 * (size_t)(b ? b->max_nat : 0);
   const int32_t rc = gb_check(b, epsilon, kernel, smem);
   if (rc != DXTB_OK) return rc;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_born_matrix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_born_matrix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DXTB_ERR_LAUNCH;
   const GbPar p = gb_par(epsilon, kernel, alpb, born_scale, born_offset);
   k_born_matrix<<<b->nmol, 256, smem, (cudaStream_t)stream>>>(*b, par_f, p, born, psi, gb_mat);
   DXTB_CHECK_LAUNCH();
@@ -323,8 +324,9 @@ extern "C" int32_t dxtb_born_gradient(const dxtb_batch *b, const double *par_f,
       sizeof(double) * 7 * (size_t)(b ? b->max_nat : 0) + sizeof(int) * (size_t)((b ? b->max_nat : 0) + 1);
   const int32_t rc = gb_check(b, epsilon, kernel, smem);
   if (rc != DXTB_OK) return rc;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_born_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_born_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DXTB_ERR_LAUNCH;
   const GbPar p = gb_par(epsilon, kernel, alpb, born_scale, born_offset);
   k_born_grad<<<b->nmol, 256, smem, (cudaStream_t)stream>>>(*b, par_f, p, q, born, psi, grad);
   DXTB_CHECK_LAUNCH();

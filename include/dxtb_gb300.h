@@ -271,7 +271,7 @@ int32_t dxtb_scf_gradient(const dxtb_batch *b, const double *par_f,
  * calculators/types/autograd.py:84-196 and scf/implicit/fixed_point.py).
  * Accumulates into grad (caller zeroes it). The GFN2 multipole terms are
  * included iff dipole is non-null; then mrad, dp, qp, vdp and vqp are
- * required. No host synchronisation (capturable in a CUDA graph). */
+ * required. No host synchronisation. */
 int32_t dxtb_gradient(const dxtb_batch *b, const double *par_f,
                       const int32_t *par_i, const double *cn,
                       const double *cn_mp, const double *mrad,
@@ -311,23 +311,26 @@ int32_t dxtb_born_gradient(const dxtb_batch *b, const double *par_f,
                            double *grad, void *stream);
 
 /* SCF without any device allocation. No counterpart in the reference: it is
- * for callers that cannot call cudaMalloc (code running under someone
- * else's stream capture, hosts that forbid allocations outside a fixed
- * pool, plugin hosts without access to an allocator). It runs the kernel of
- * dxtb_scf with the same inputs and outputs, but takes its scratch
- * workspace from a fixed array inside the library (DXTB_NOALLOC_SCRATCH_
- * DOUBLES doubles = 16 MiB per GPU that loads the library, held until the
- * process exits) instead of caller memory. A batch whose workspace
- * (sum over molecules of dxtb_scf_workspace_mol plus nmol + 2 header words)
- * does not fit returns DXTB_ERR_TOO_LARGE without running.
+ * for callers that must not call cudaMalloc, such as hosts that hand the
+ * library a fixed device-memory pool and forbid allocations outside it, or
+ * plugin hosts whose allocator cannot be reached through a C ABI. It runs
+ * the kernels of dxtb_scf with the same inputs and outputs, but takes its
+ * scratch workspace from a fixed array inside the library
+ * (DXTB_NOALLOC_SCRATCH_DOUBLES doubles = 16 MiB on every GPU that loads
+ * the library, held until the process exits) instead of caller memory.
+ * The array starts with a header of H = 32 * ceil((nmol + 2) / 32) int64
+ * words (the total size and the per-molecule offsets); a batch whose
+ * H + sum over molecules of dxtb_scf_workspace_mol exceeds the array
+ * returns DXTB_ERR_TOO_LARGE without running the SCF.
+ * Every call computes that size on the device, copies it to the host and
+ * synchronises the caller's stream once before it launches the SCF.
  * The first call on a device looks up the array's device address, and the
- * first call from each CUDA stream creates that stream's side stream and
- * fork/join events for the large-molecule kernel (set-up, no device
- * memory); make those first calls before any stream capture. All calls share the one
- * array, which keeps the last call's contents (nothing in it needs to start
- * at zero): calls that overlap on the GPU (other streams, other threads)
- * race and must be serialised by the caller. The call synchronises the
- * stream once to check the size. */
+ * first call from each CUDA stream creates that stream's side streams and
+ * fork/join events for the larger size classes (set-up only, no device
+ * memory); make that first call before any stream capture begins. All calls
+ * share the one array, which keeps the last call's contents (nothing in it
+ * needs to start at zero): calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller. */
 #define DXTB_NOALLOC_SCRATCH_DOUBLES (1 << 21)
 int32_t dxtb_scf_noalloc(const dxtb_batch *b, const double *par_f,
                          const int32_t *par_i, const double *overlap,

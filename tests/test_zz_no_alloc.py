@@ -1,9 +1,13 @@
 """
-dxtb_scf_noalloc: the SCF entry point for callers that cannot allocate
-device memory (stream-capturing hosts, fixed-pool hosts, plugin hosts
-without an allocator). Called through the C ABI, its results must equal
-those of dxtb_scf on the same inputs, on two calls in a row (the shared
-scratch array keeps the first call's contents when the second starts).
+dxtb_scf_noalloc: the SCF entry point for callers that must not allocate
+device memory (hosts that give the library a fixed pool and forbid other
+allocations, plugin hosts whose allocator the C ABI cannot reach). Called
+through the C ABI, its results must equal those of dxtb_scf on the same
+inputs, on two calls in a row (the shared scratch array keeps the first
+call's contents when the second starts). The batch holds small molecules
+and one of at least 136 orbitals, so the one-SM or cluster classes, which
+run on side streams forked from the caller's stream, read the scratch
+header too.
 
 This file is collected last so that a failure here never hides another test.
 """
@@ -26,15 +30,15 @@ def test_noalloc_scf_matches_allocating_entry_point():
     from dxtb_gb300.engine import PackedBatch, run
     from dxtb_gb300.workloads import random_molecule
 
-    mols = [random_molecule(5000 + i, n) for i, n in enumerate([9, 17, 26])]
+    mols = [random_molecule(5000 + i, n) for i, n in enumerate([9, 17, 26, 58])]
     pb = PackedBatch(tables("gfn2"), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols])
+    L = _lib.lib()
+    thr = (C.c_int32 * 5)()
+    assert L.dxtb_scf_get_size_classes(thr) == 0
+    assert int(pb.nao.max()) >= thr[1]  # a one-SM or cluster class is in the batch
     ref = run(pb, forces=True)
     s = ref.state
     assert (ref.status.cpu() == 0).all()
-    L = _lib.lib()
-    L.dxtb_scf_noalloc.restype = C.c_int32
-    L.dxtb_scf_noalloc.argtypes = [C.c_void_p] * 15 + [C.c_double, C.c_int32, C.c_double] + \
-        [C.c_void_p] * 15
     tot = pb.total
     nm, no, na = tot["mat"], tot["aos"], tot["atoms"]
     dev = pb.device
@@ -77,9 +81,6 @@ def test_noalloc_rejects_oversized_batch():
     pb = PackedBatch(tables("gfn2"), [num], [torch.tensor(pos)])
     assert int(pb.nao[0]) > 836
     L = _lib.lib()
-    L.dxtb_scf_noalloc.restype = C.c_int32
-    L.dxtb_scf_noalloc.argtypes = [C.c_void_p] * 15 + [C.c_double, C.c_int32, C.c_double] + \
-        [C.c_void_p] * 15
     dummy = torch.zeros(1, dtype=torch.float64, device=pb.device)
     p = dummy.data_ptr()
     rc = L.dxtb_scf_noalloc(C.byref(pb.struct), pb.t["par_f"].data_ptr(), pb.t["par_i"].data_ptr(),
