@@ -45,8 +45,10 @@ def args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--count", type=int, default=256)
-    p.add_argument("--cpu-sample", type=int, default=12, help="molecules timed on the CPU")
-    p.add_argument("--per-molecule", type=int, default=16, help="molecules on the 1-by-1 GPU path")
+    p.add_argument("--cpu-sample", type=int, default=16,
+                   help="molecules timed on the CPU (at the size quantiles of the set)")
+    p.add_argument("--per-molecule", type=int, default=16,
+                   help="molecules on the 1-by-1 GPU path (at the size quantiles of the set)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--serve-rate", type=float, default=2000.0,
                    help="Poisson arrival rate of the serving leg (0: skip the leg)")
@@ -123,26 +125,63 @@ class Clocks:
         }
 
 
-def fp64_peak_tflops(dev) -> float:
-    """Measured FP64 FMA rate of this GPU (TFLOP/s)."""
+MMA_SHAPES = {0: (8, 8, 4), 1: (16, 8, 4), 2: (16, 8, 8), 3: (16, 8, 16)}
+
+
+def fp64_peaks(dev, local: int) -> dict:
+    """
+    Measured FP64 rates of this GPU (TFLOP/s), with the SM clock sampled
+    while the probes run (about a second in total): the scalar FMA pipe
+    (``dxtb_fp64_fma_probe``, the roofline denominator of the SCF) and the
+    FP64 tensor-core instructions (``dxtb_fp64_mma_probe``, one entry per
+    mma.sync shape).
+    """
     from dxtb_gb300 import _lib
 
     L = _lib.lib()
     out = torch.zeros(1, dtype=torch.float64, device=dev)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    blocks, threads, iters = sms * 8, 256, 20000
     st = _lib.stream_ptr()
-    for _ in range(2):
-        _lib.check(L.dxtb_fp64_fma_probe(iters, blocks, threads, out.data_ptr(), st), "probe")
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(3):
-        s.record()
-        _lib.check(L.dxtb_fp64_fma_probe(iters, blocks, threads, out.data_ptr(), st), "probe")
-        e.record()
-        e.synchronize()
-        best = max(best, 2.0 * 8 * iters * blocks * threads / (s.elapsed_time(e) * 1e-3) / 1e12)
-    return best
+    blocks, threads = sms * 8, 256
+
+    def rate(launch, flops, reps=3):
+        launch()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = 0.0
+        for _ in range(reps):
+            s.record()
+            launch()
+            e.record()
+            e.synchronize()
+            best = max(best, flops / (s.elapsed_time(e) * 1e-3) / 1e12)
+        return best
+
+    clocks = Clocks(local)
+    t0 = time.perf_counter()
+    out_d: dict = {}
+    while True:
+        iters = 40000
+        fma = rate(lambda: _lib.check(L.dxtb_fp64_fma_probe(iters, blocks, threads, out.data_ptr(), st),
+                                      "probe"), 2.0 * 8 * iters * blocks * threads)
+        out_d["dfma"] = max(out_d.get("dfma", 0.0), fma)
+        for sh, (m, n, k) in MMA_SHAPES.items():
+            it = 4000
+            r = rate(lambda: _lib.check(L.dxtb_fp64_mma_probe(sh, it, blocks, threads, out.data_ptr(), st),
+                                        "probe"), 2.0 * m * n * k * 4 * it * (threads // 32) * blocks)
+            key = f"dmma_m{m}n{n}k{k}"
+            out_d[key] = max(out_d.get(key, 0.0), r)
+        if time.perf_counter() - t0 > 1.0:
+            break
+    out_d["clocks"] = clocks.stop()
+    return out_d
+
+
+def quantile_sample(nao: np.ndarray, k: int) -> list[int]:
+    """k molecules at the size quantiles of the set (sorted by orbital count,
+    the middle of each of k equal slices): their mean n^3 matches the set's."""
+    o = np.argsort(nao, kind="stable")
+    k = min(k, len(nao))
+    return [int(o[int((j + 0.5) * len(nao) / k)]) for j in range(k)]
 
 
 def scf_flops(nao: np.ndarray, iters: np.ndarray, forces: bool) -> float:
@@ -153,12 +192,20 @@ def scf_flops(nao: np.ndarray, iters: np.ndarray, forces: bool) -> float:
     return float(((2.0 / 3.0) + iters * (34.0 / 3.0) + (2.0 if forces else 0.0)) @ n3)
 
 
+def nao_of(mols) -> np.ndarray:
+    """GFN2 orbital counts of a molecule list (H 1, C/N/O/F 4, S 9)."""
+    ao = {1: 1, 6: 4, 7: 4, 8: 4, 9: 4, 16: 9}
+    return np.array([sum(ao[int(z)] for z in m[0]) for m in mols], dtype=np.int64)
+
+
 def cpu_reference(mols, sample: int, method="gfn2"):
-    """The CPU restatement of the reference path (oracle), E + F per molecule."""
+    """The CPU restatement of the reference path (oracle), E + F per molecule,
+    on `sample` molecules at the size quantiles of the set."""
     from oracle import xtb_oracle as X
 
     threads = torch.get_num_threads()
-    sel = mols[:sample]
+    idx = quantile_sample(nao_of(mols), sample)
+    sel = [mols[i] for i in idx]
     times, energies = [], []
     t0 = time.perf_counter()
     for num, pos in sel:
@@ -172,10 +219,46 @@ def cpu_reference(mols, sample: int, method="gfn2"):
         "unit": "molecules/s",
         "cores": threads,
         "kind": "port",
-        "sample": f"first {len(sel)} of the {len(mols)} molecules, sequential, E+F, float64",
+        "sample": (f"{len(sel)} of the {len(mols)} molecules at the size quantiles (mean n^3 "
+                   f"{np.mean(nao_of(sel).astype(float) ** 3) / np.mean(nao_of(mols).astype(float) ** 3):.3f}"
+                   " x the set's), sequential, E+F, float64"),
         "p50_ms": 1e3 * float(np.percentile(times, 50)),
         "p99_ms": 1e3 * float(np.percentile(times, 99)),
-    }, energies
+    }, dict(zip(idx, energies))
+
+
+# DRAM bytes (read + write) of the SCF launches per step, from the ncu
+# capture of the SCF kernels summarised under profiles/ (None until measured)
+SCF_TRAFFIC = None
+SCF_TRAFFIC_SOURCE = None
+
+
+def measured_hbm_gbs() -> float | None:
+    """HBM copy bandwidth of this machine's GPUs (MEASURED_PEAKS.json), if present."""
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(f.read_text())["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def set_parity(res, pb) -> dict:
+    """Energies and forces of every molecule of the timed batch against the
+    oracle fixture of the 256-molecule set (tests/golden/sets_c2.npz)."""
+    d = np.load(ROOT / "tests" / "golden" / "sets_c2.npz")
+    e = res.energy.cpu().numpy()
+    g = res.gradient.cpu().numpy()
+    de = np.abs(e - d["gfn2/energy"])
+    df = np.array([np.abs(g[pb.atom_off[i]: pb.atom_off[i + 1]] - d["gfn2/gradient"][i, : d["nat"][i]]).max()
+                   for i in range(pb.nmol)])
+    return {
+        "molecules": int(pb.nmol),
+        "max_abs_dE": float(de.max()),
+        "max_abs_dF": float(df.max()),
+        "outside_tol": int(((de > 1e-8) | (df > 1e-6)).sum()),
+        "tol": {"dE_Eh": 1e-8, "dF_Eh_per_bohr": 1e-6},
+        "reference": "oracle float64 (tol 1e-10), all molecules of the set",
+    }
 
 
 def main():
@@ -249,14 +332,22 @@ def main():
     iters = res.iterations.cpu().numpy()
     value = pb.nmol * a.steps * world / total_s
 
-    # roofline of the dominant kernel (the persistent SCF launch)
-    peak = fp64_peak_tflops(dev)
+    # parity of the timed result on every molecule against the oracle fixture
+    parity = set_parity(res, pb) if a.count == 256 else None
+
+    # roofline of the dominant kernels (the persistent SCF launches)
+    peaks = fp64_peaks(dev, local)
+    peak = peaks["dfma"]
     flops = scf_flops(pb.nao, iters, True)
     achieved = flops / (stages["scf"] * 1e-3) / 1e12
+    # integral stage: S, H0, D (3) and Q (6) written, 8 bytes each per n^2
+    int_bytes = 8.0 * 11 * float((pb.nao.astype(np.float64) ** 2).sum())
+    hbm_peak = measured_hbm_gbs()
+    int_gbs = int_bytes / (stages["integrals"] * 1e-3) / 1e9
 
     # per-molecule GPU path (same kernels, one molecule per launch)
     per = []
-    for i in range(min(a.per_molecule, pb.nmol)):
+    for i in quantile_sample(pb.nao, a.per_molecule):
         pbi = PackedBatch(tables("gfn2"), [nums[i]], [pos[i]], dev)
         sti: dict = {}
         run(pbi, forces=True, state=sti)
@@ -327,11 +418,10 @@ def main():
                         "hbm_budget_gb": 120.0, "status_bad": sum(1 for r in out if r.status != 0)})
 
     cpu_baseline = None
-    max_de = None
     if rank == 0 and a.cpu_sample > 0:
         cpu_baseline, ref_e = cpu_reference(mols, a.cpu_sample)
-        got = res.energy.cpu().numpy()[: len(ref_e)]
-        max_de = float(np.abs(got - np.array(ref_e)).max())
+        got = res.energy.cpu().numpy()
+        cpu_baseline["max_abs_dE_vs_gpu"] = float(max(abs(got[i] - e) for i, e in ref_e.items()))
     if rank != 0:
         return
     line = {
@@ -365,17 +455,25 @@ def main():
                          "p50_ms": float(np.percentile(per, 50)) if per else None,
                          "p99_ms": float(np.percentile(per, 99)) if per else None},
         "speedup_vs_per_molecule": value / per_mol_value if per_mol_value else None,
-        "parity": {"max_abs_dE_vs_cpu_reference_sample": max_de},
+        "parity": parity,
         "roofline": {
-            "kernel": "k_scf (persistent SCF, one CTA per molecule)",
+            "kernel": ("SCF launches k_scf<256,2>, k_scf<512,1>, k_scf_cluster (a CTA or a "
+                       "cluster of 2-16 CTAs per molecule, by size class), over the SCF stage"),
             "bound": "fp64",
             "achieved": achieved,
             "peak": peak,
             "unit": "TFLOP/s",
             "frac": achieved / peak,
-            "peak_source": "measured FP64 FMA probe (dxtb_fp64_fma_probe) on this GPU",
-            "traffic": None,
+            "peak_source": "measured FP64 FMA probe (dxtb_fp64_fma_probe) on this GPU, best of the probe runs",
+            "traffic": SCF_TRAFFIC,
+            "traffic_source": SCF_TRAFFIC_SOURCE,
         },
+        "stage_roofline": {
+            "scf": {"bound": "fp64", "achieved_tflops": achieved, "frac_of_dfma": achieved / peak},
+            "integrals": {"bound": "hbm", "bytes_written": int_bytes, "achieved_gbs": int_gbs,
+                          "peak_gbs": hbm_peak, "frac": int_gbs / hbm_peak if hbm_peak else None},
+        },
+        "fp64_probes_tflops": peaks,
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
         "serving": serving,

@@ -60,6 +60,7 @@ _SIGS = {
     "dxtb_born_matrix": (i32, [vp, vp, vp, f64, i32, i32, f64, f64, vp, vp, vp, vp]),
     "dxtb_born_gradient": (i32, [vp, vp, vp, f64, i32, i32, f64, f64, vp, vp, vp, vp, vp]),
     "dxtb_fp64_fma_probe": (i32, [i64, i32, i32, vp, vp]),
+    "dxtb_fp64_mma_probe": (i32, [i32, i64, i32, i32, vp, vp]),
     "dxtb_scf_noalloc": (i32, [vp] * 15 + [f64, i32, f64] + [vp] * 15),
 }
 

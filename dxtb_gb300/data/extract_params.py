@@ -91,4 +91,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python -m dxtb_gb300.data.extract_params <path to the dxtb source tree>")
+    main(sys.argv[1])

@@ -352,6 +352,14 @@ int32_t dxtb_scf_noalloc(const dxtb_batch *b, const double *par_f,
 int32_t dxtb_fp64_fma_probe(int64_t iters, int32_t blocks, int32_t threads,
                             double *out, void *stream);
 
+/* FP64 tensor-core (DMMA) throughput probe: every warp of blocks x threads
+ * runs 4 independent accumulator chains of iters mma.sync f64 instructions
+ * of one shape (0 = m8n8k4, 1 = m16n8k4, 2 = m16n8k8, 3 = m16n8k16);
+ * flops = 2 M N K * 4 * iters * threads / 32 * blocks. threads must be a
+ * multiple of 32. No counterpart in the reference. */
+int32_t dxtb_fp64_mma_probe(int32_t shape, int64_t iters, int32_t blocks,
+                            int32_t threads, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,34 @@ def _refs_dict(src: str, var: str = "refs") -> dict[str, dict[str, np.ndarray]]:
     raise KeyError(var)
 
 
+def _flat_literal(node) -> list[float]:
+    """Numbers of a list literal whose items may be starred sub-lists."""
+    out: list[float] = []
+    for el in node.elts:
+        if isinstance(el, ast.Starred):
+            out.extend(_flat_literal(el.value))
+        elif isinstance(el, (ast.List, ast.Tuple)):
+            out.extend(_flat_literal(el))
+        else:
+            out.append(float(ast.literal_eval(el)))
+    return out
+
+
+def _reshaped_tensor_dict(src: str, var: str = "ref") -> dict[str, np.ndarray]:
+    """The module-level ``{name: torch.tensor([...]).reshape(r, c)}`` dict ``var``."""
+    tree = ast.parse(src)
+    for node in tree.body:
+        tgt = getattr(node, "target", None) or (getattr(node, "targets", [None]) or [None])[0]
+        if isinstance(node, (ast.Assign, ast.AnnAssign)) and isinstance(tgt, ast.Name) and tgt.id == var:
+            out = {}
+            for kn, vn in zip(node.value.keys, node.value.values):
+                shape = tuple(int(ast.literal_eval(a)) for a in vn.args)
+                vals = _flat_literal(vn.func.value.args[0])
+                out[kn.value] = np.array(vals, dtype=np.float64).reshape(shape)
+            return out
+    raise KeyError(var)
+
+
 def main(ref_root: str) -> None:
     root = Path(ref_root)
     test = root / "test"
@@ -140,9 +168,18 @@ def main(ref_root: str) -> None:
         "eps 78.9), energies_still (GB Still), charges, gsolv and gradient (GFN1 + ALPB)"
     )
     src["MB16_43_01/*"] = "test/test_singlepoint/mols/MB16_43_01/coord"
+    # GFN2 H0 without the overlap factor (tblite 0.3.0), H2, LiH and SiH4
+    h2 = _reshaped_tensor_dict((test / "test_hamiltonian" / "test_gfn2.py").read_text())
+    for m in ("H2", "LiH", "SiH4"):
+        g[f"{m}/h0scale_gfn2"] = h2[m]
+    src["*/h0scale_gfn2"] = (
+        "test/test_hamiltonian/test_gfn2.py ref (tblite 0.3.0): GFN2 H0 built with overlap=None"
+    )
     np.savez_compressed(HERE / "golden.npz", **g)
     (HERE / "golden_sources.json").write_text(json.dumps(src, indent=1))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the dxtb source tree>")
+    main(sys.argv[1])

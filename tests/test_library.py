@@ -25,6 +25,15 @@ def test_library_exports_header_symbols():
     assert not missing, missing
 
 
+def test_bindings_cover_header_symbols():
+    """Every declared entry point has ctypes argtypes (doubles and int64
+    arguments would otherwise be passed as C ints)."""
+    from dxtb_gb300 import _lib
+
+    missing = [s for s in _declared() if s not in _lib._SIGS]
+    assert not missing, missing
+
+
 def test_layout_parsed_from_header():
     from dxtb_gb300.params import layout
 

@@ -33,6 +33,23 @@ def test_overlap_and_h0_gfn1(name):
     assert np.abs(h.numpy() - G[f"{name}/h0_gfn1"]).max() < 2e-7
 
 
+@pytest.mark.parametrize("name", ["H2", "LiH", "SiH4"])
+def test_h0_gfn2_without_overlap(name):
+    """test/test_hamiltonian/test_gfn2.py inline references (tblite 0.3.0):
+    the GFN2 H0 built with overlap=None, i.e. the scaling matrix (self-energies
+    with the GFN2 CN shift, wexp/Slater factor, shell and pair scaling, EN
+    term, distance polynomial). Reference tolerance sqrt(eps) * 10."""
+    num, pos = mol(name)
+    sysm = X.make_system("gfn2", num)
+    p = torch.tensor(pos)
+    cn = X.coordination_number(num, p, "gfn")
+    n = sysm.nao
+    h = X.hamiltonian(sysm, p, torch.ones(n, n, dtype=torch.float64), cn)
+    ref = G[f"{name}/h0scale_gfn2"]
+    assert h.shape == ref.shape
+    assert np.abs(h.numpy() - ref).max() < np.sqrt(np.finfo(np.float64).eps) * 10
+
+
 def test_planted_radius_error_is_caught(monkeypatch):
     """A 1 % error in one atomic radius of the oracle breaks the H0 pin."""
     from dxtb_gb300.data import radii
