@@ -43,16 +43,28 @@ class Batch(C.Structure):
     ]
 
 
+class ScfConfig(C.Structure):
+    """Mirror of ``dxtb_scf_config``."""
+
+    _fields_ = [
+        ("maxiter", i32), ("mixer", i32), ("x_atol", f64), ("f_atol", f64), ("x_atol_max", f64),
+        ("damp", f64), ("damp_init", f64), ("generations", i32), ("soft_start", i32),
+        ("diagonal_offset", f64),
+    ]
+
+
+MIXERS = {"broyden1": 0, "anderson": 1}
+
+
 _SIGS = {
     "dxtb_coordination_number": (i32, [vp, vp, vp, i32, vp, vp]),
     "dxtb_interaction_cache": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "dxtb_multipole_h0": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "dxtb_multipole_raw": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     "dxtb_scf_workspace_mol": (i64, [i64, i64]),
-    "dxtb_scf": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, f64,
-                       vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "dxtb_scf": (i32, [vp] * 15 + [f64, vp] + [vp] * 17),
     "dxtb_gradient": (i32, [vp] * 22),
-    "dxtb_scf_gradient": (i32, [vp] * 15 + [f64, i32, f64] + [vp] * 21),
+    "dxtb_scf_gradient": (i32, [vp] * 15 + [f64, vp] + [vp] * 21),
     "dxtb_index_sizes": (i32, [vp, i32, i32, i32, vp, vp, vp]),
     "dxtb_index_maps": (i32, [vp, i32, i32, i32, vp, vp, i64, i64] + [vp] * 14 + [vp]),
     "dxtb_scf_set_size_classes": (i32, [vp]),

@@ -17,6 +17,18 @@ the positions as in the reference.
 Not computed (the reference's defaults include them): D3/D4 dispersion and
 the GFN1 halogen-bond term; callers wanting parity pass
 ``opts={"exclude": ["disp", "hal"]}`` to the reference.
+
+SCF options follow the reference's ConfigSCF (constants/defaults.py):
+``scf_mode`` "full" (default; the loop of scf/unrolling with the Anderson
+mixer, to which the default ``mixer="broyden"`` falls back there, with a
+warning, as in scf/unrolling/base.py:80-96) or "implicit" (the xitorch
+broyden1 root solver of scf/implicit); ``maxiter`` 100, ``x_atol`` and
+``f_atol`` 1e-4, ``x_atol_max`` 1e-5, ``damp`` 0.5, ``damp_init`` 0.1,
+``damp_generations`` 5, ``damp_soft_start`` True, ``damp_diagonal_offset``
+0.01, ``fermi_etemp`` 300 K. Options the GB300 path does not honour warn or
+raise: the EEQ guess (the reference default; the zero-potential SAD start is
+used), the linear mixer, SCP modes other than the potential, integral
+drivers other than the PyTorch one (the GB300 kernels give its integrals).
 """
 
 from __future__ import annotations
@@ -46,6 +58,45 @@ class SCFConvergenceError(RuntimeError):
 
 class SCFConvergenceWarning(UserWarning):
     """SCF did not converge within ``maxiter``."""
+
+
+# option strings of the reference (constants/labels/scf.py, integrals.py)
+_SCF_FULL = ("full", "full_tracking", "unrolling")
+_SCF_IMPLICIT = ("default", "implicit")
+_MIXER_ANDERSON = ("anderson", "a")
+_MIXER_BROYDEN = ("broyden", "b")
+_MIXER_LINEAR = ("linear", "l", "simple", "s")
+_GUESS_SAD = ("sad", "zero")
+_GUESS_EEQ = ("eeq", "equilibration")
+_INT_PYTORCH = ("autograd", "pytorch", "torch", "dxtb")
+_INT_LIBCINT = ("libcint", "c")
+_GRAD_MODES = ("autograd", "backward", "functorch", "row")
+# constants/defaults.py
+_DEFAULTS = {"maxiter": 100, "x_atol": 1e-4, "f_atol": 1e-4, "x_atol_max": 1e-5, "damp": 0.5,
+             "damp_init": 0.1, "damp_generations": 5, "damp_soft_start": True,
+             "damp_diagonal_offset": 0.01, "fermi_etemp": 300.0}
+
+
+def _opt_str(v) -> str:
+    return str(v).lower() if not isinstance(v, int) else str(v)
+
+
+class Result:
+    """
+    Single-point results with the attribute names of the reference's Result
+    (calculators/result.py:36-120). Energies are per molecule (scalars for
+    one molecule, (B,) for a batch) where the reference keeps atom-resolved
+    tensors; ``cenergies`` holds the repulsion. ``charges``, ``emo`` and
+    ``occupation`` are orbital vectors, ``density`` and ``coefficients`` the
+    n x n matrices (zero-padded to (B, n, n) for a batch; orbital j is
+    column j of ``coefficients``, as in the reference).
+    """
+
+    __slots__ = ["charges", "coefficients", "cenergies", "density", "emo", "fenergy", "iter",
+                 "occupation", "scf", "total"]
+
+    def get_energies(self) -> dict:
+        return {"total": self.total, "scf": self.scf, "fenergy": self.fenergy, **self.cenergies}
 
 
 _TABLES: dict[str, Tables] = {}
@@ -90,15 +141,19 @@ class Calculator:
             numbers = torch.as_tensor(numbers)
         if numbers.dtype not in (torch.int16, torch.int32, torch.int64):
             raise DtypeError(f"Atomic numbers must be integers, got {numbers.dtype}")
-        self.device = torch.device(device) if device is not None else numbers.device
+        # device None: the current CUDA device (this path has no CPU variant)
+        self.device = torch.device(device) if device is not None else torch.device("cuda")
         if self.device.type != "cuda":
-            self.device = torch.device("cuda")
+            raise DeviceError(
+                f"the GB300 path runs on a CUDA device only, got device {self.device}"
+            )
         self.dtype = dtype or torch.float64
         if self.dtype != torch.float64:
             raise DtypeError("the GB300 path computes in float64 only")
         self.numbers = numbers
         self.batched = numbers.ndim > 1
         self.opts = dict(opts or {})
+        self._scf = self._scf_options()
         self.solvation = solvation
         if interaction is not None:
             from .solvation import GeneralizedBorn
@@ -132,18 +187,68 @@ class Calculator:
         self._state: dict = {}
         self._cache: dict = {}
 
-    # ---- configuration (constants/defaults.py) ----
+    # ---- configuration (constants/defaults.py, calculators/config/scf.py) ----
+    def _opt(self, key):
+        return self.opts.get(key, _DEFAULTS.get(key))
+
+    def _scf_options(self) -> dict:
+        """The SCF configuration of ``opts`` (reference defaults where unset),
+        with warnings or errors for what the GB300 path does not honour."""
+        mode = _opt_str(self.opts.get("scf_mode", "full"))
+        mixer = _opt_str(self.opts.get("mixer", "broyden"))
+        if mode in _SCF_FULL or mode == "0":
+            if mixer in _MIXER_LINEAR or mixer == "0":
+                raise NotImplementedError("the linear (simple) mixer is not on the GB300 path")
+            if mixer in _MIXER_BROYDEN or mixer == "2":
+                # scf/unrolling/base.py:80-96: Broyden falls back to Anderson in full mode
+                warnings.warn("Broyden mixer is not implemented for SCF with full gradient "
+                              "tracking. Using Anderson mixer instead.", stacklevel=3)
+            elif not (mixer in _MIXER_ANDERSON or mixer == "1"):
+                raise ValueError(f"Unknown mixer '{mixer}'.")
+            kind = "anderson"
+        elif mode in _SCF_IMPLICIT or mode == "1":
+            kind = "broyden1"  # scf/implicit: xitorch broyden1 whatever the mixer
+        else:
+            raise NotImplementedError(f"SCF mode '{mode}' is not on the GB300 path")
+        scp = _opt_str(self.opts.get("scp_mode", "potential"))
+        if scp not in ("potential", "pot", "2"):
+            raise NotImplementedError(f"SCP mode '{scp}': the GB300 SCF iterates on the potential")
+        guess = _opt_str(self.opts.get("guess", "eeq"))
+        if guess in _GUESS_EEQ or guess == "0":
+            warnings.warn("the EEQ initial guess is not on the GB300 path; the SAD guess (zero "
+                          "charges, zero potential) is used", stacklevel=3)
+        elif not (guess in _GUESS_SAD or guess == "1"):
+            raise ValueError(f"Unknown guess '{guess}'.")
+        drv = _opt_str(self.opts.get("int_driver", "pytorch"))
+        if drv in _INT_LIBCINT or drv == "0":
+            warnings.warn("the libcint integral driver is not on the GB300 path; the GB300 "
+                          "McMurchie-Davidson kernels (equal to the PyTorch driver) are used",
+                          stacklevel=3)
+        elif not (drv in _INT_PYTORCH or drv == "1"):
+            raise ValueError(f"Unknown integral driver '{drv}'.")
+        return {
+            "mixer": kind,
+            "x_atol": float(self._opt("x_atol")),
+            "f_atol": float(self._opt("f_atol")),
+            "x_atol_max": float(self._opt("x_atol_max")),
+            "damp": float(self._opt("damp")),
+            "damp_init": float(self._opt("damp_init")),
+            "generations": int(self._opt("damp_generations")),
+            "soft_start": bool(self._opt("damp_soft_start")),
+            "diagonal_offset": float(self._opt("damp_diagonal_offset")),
+        }
+
     @property
     def maxiter(self) -> int:
-        return int(self.opts.get("maxiter", 250))
+        return int(self._opt("maxiter"))
 
     @property
     def etemp(self) -> float:
-        return float(self.opts.get("fermi_etemp", 300.0))
+        return float(self._opt("fermi_etemp"))
 
     @property
     def tol(self) -> float:
-        return float(self.opts.get("x_atol", self.opts.get("f_atol", 1e-10)))
+        return self._scf["x_atol"]
 
     def reset(self) -> None:
         """Forget cached results (types/base.py:758-763)."""
@@ -192,7 +297,7 @@ class Calculator:
         else:
             self._pb.set_positions(plist)
         res = engine.run(self._pb, etemp=self.etemp, maxiter=self.maxiter, tol=self.tol,
-                         forces=forces, gb=self.solvation, state=self._state)
+                         forces=forces, gb=self.solvation, state=self._state, scf=self._scf)
         st = res.status.cpu()
         bad = st[(st != 0)]
         if len(bad):
@@ -229,22 +334,55 @@ class Calculator:
         return self._run(positions, chrg, spin)["energy"]
 
     def get_forces(self, positions, chrg=0, spin=None, grad_mode="autograd", **_):
+        """-dE/dR. Every ``grad_mode`` of the reference (autograd, backward,
+        functorch, row; calculators/types/autograd.py:146-196) gives the same
+        forces here: they come from the adjoint kernels."""
+        if grad_mode not in _GRAD_MODES:
+            raise ValueError(f"Unknown grad_mode '{grad_mode}'.")
         return self.forces(positions, chrg, spin)
 
     def forces(self, positions, chrg=0, spin=None):
         r = self._run(positions.detach(), chrg, spin, forces=True)
         return -r["gradient"]
 
-    def singlepoint(self, positions, chrg=0, spin=None):
+    def singlepoint(self, positions, chrg=0, spin=None) -> Result:
+        """The single point as a ``Result`` (calculators/types/energy.py:78-414)."""
         r = self._run(positions.detach(), chrg, spin)
         res = r["result"]
-        return {
-            "energy": r["energy"],
-            "scf": res.e_scf if self.batched else res.e_scf[0],
-            "fenergy": res.e_free if self.batched else res.e_free[0],
-            "repulsion": res.e_rep if self.batched else res.e_rep[0],
-            "iterations": res.iterations,
-        }
+        pb = self._pb
+        st = res.state
+        one = not self.batched
+
+        def per_mol(v):
+            return v[0] if one else v
+
+        out = Result()
+        out.total = r["energy"]
+        out.scf = per_mol(res.e_scf)
+        out.fenergy = per_mol(res.e_free)
+        out.cenergies = {"repulsion": per_mol(res.e_rep)}
+        out.iter = res.iterations.to(torch.int64)
+        nmax = int(pb.nao.max())
+        vec = {k: torch.zeros(pb.nmol, nmax, dtype=torch.float64, device=pb.device)
+               for k in ("q", "evals", "occ")}
+        mat = {k: torch.zeros(pb.nmol, nmax, nmax, dtype=torch.float64, device=pb.device)
+               for k in ("P", "C")}
+        for i in range(pb.nmol):
+            n, o0, m0 = int(pb.nao[i]), int(pb.ao_off[i]), int(pb.mat_off[i])
+            for k in vec:
+                vec[k][i, :n] = st[k][o0 : o0 + n]
+            order = torch.argsort(vec["evals"][i, :n])
+            vec["evals"][i, :n] = vec["evals"][i, :n][order]
+            vec["occ"][i, :n] = vec["occ"][i, :n][order]
+            mat["P"][i, :n, :n] = st["P"][m0 : m0 + n * n].view(n, n)
+            # rows of the C block are orbitals (unsorted); columns here
+            mat["C"][i, :n, :n] = st["C"][m0 : m0 + n * n].view(n, n)[order].T
+        out.charges = per_mol(vec["q"])
+        out.emo = per_mol(vec["evals"])
+        out.occupation = per_mol(vec["occ"])
+        out.density = per_mol(mat["P"])
+        out.coefficients = per_mol(mat["C"])
+        return out
 
 
 class GFN1Calculator(Calculator):

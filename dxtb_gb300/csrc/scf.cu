@@ -22,7 +22,6 @@ namespace dxtb {
 constexpr int kScfThreads = 256;     // CTA size for molecules sharing an SM
 constexpr int kScfBigThreads = 512;  // CTA size of one-SM and cluster teams
 constexpr int kRank = 256;           // Broyden memory (the reference keeps every update; >= maxiter)
-constexpr double kDamp = 0.5;        // step damping of the root solver (defaults.DAMP)
 constexpr double kOccCut = 1e-15;    // orbitals below this occupation carry no density
 constexpr int kLuSlots = 1024;       // concurrent inverse-iteration factorisations per molecule
 // size classes (kClasses, common.cuh): 0 small, 1 one SM, 2..5 clusters of 2..16
@@ -85,7 +84,7 @@ __device__ inline Ws ws_carve(double *base, int n, int nat) {
   w.lu = q; q += (size_t)lu_size(n);
   w.cl = reinterpret_cast<int *>(q); q += n + 8;
   w.sdot = q; q += 4 * kRank + 64;
-  w.team = q; q += 64;  // [0, 32) partial sums, [32, 48) broadcast words (int)
+  w.team = q; q += 64;  // [0, 32) partial sums, [32, 48) broadcast words (int), [48] mixer flag
   w.misc = q;  // 64 + 16 nat + 2N
   return w;
 }
@@ -157,6 +156,9 @@ struct ScfArgs {
   const double *S, *H0, *D, *Q, *gamma, *hd, *sd, *dd, *sq, *gb, *n0, *nel;
   double kt, xtol, ftol;
   int maxiter;
+  // root solver / mixer (dxtb_scf_config)
+  int mixer, generations, soft_start;
+  double xtol_max, damp, damp_init, offset;
   const int64_t *ws_off;
   const int32_t *order;
   double *ws, *P, *W, *C, *evals, *occ, *q, *dp, *qp, *vorb, *vdp, *vqp, *energies;
@@ -288,9 +290,11 @@ __device__ double interaction_energy(const ScfArgs &a, const MolView &mv, const 
   return block_sum(e, red);
 }
 
-// State of the root solver, held by the lead CTA only.
+// State of the root solver, held by the lead CTA only. final_eval: one more
+// pass evaluates the energy at the iterate left in x (hit_max: with status
+// MAXITER); base: the Anderson history ring's entry 0.
 struct Broyden {
-  int nrank = 0, final_eval = 0, hit_max = 0;
+  int nrank = 0, final_eval = 0, hit_max = 0, base = 0;
   double resid = 0.0, best_ynorm = 1e308, dx_norm = 0.0;
 };
 
@@ -384,6 +388,7 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
     if (br.best_ynorm < ynorm) {
       for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = w.xbest[t];
       br.final_eval = 1;
+      br.hit_max = 1;
       __syncthreads();
       return kNext;
     }
@@ -407,7 +412,7 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
     for (int k = 0; k < nrank; ++k) dx -= w.hx[(size_t)k * N + t] * sdot[k];
     w.rold[t] = y;
     w.xold[t] = w.x[t];
-    w.x[t] += kDamp * dx;
+    w.x[t] += a.damp * dx;
     pdx += dx * dx;
   }
   br.dx_norm = sqrt(block_sum(pdx, red));
@@ -415,6 +420,141 @@ __device__ int broyden_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br,
     status = DXTB_ERR_NAN;
     return kStop;
   }
+  return kNext;
+}
+
+// Solves the n x n system A th = r in place (Gaussian elimination with
+// partial pivoting, n <= kMaxGen); one thread. False for a zero pivot.
+constexpr int kMaxGen = 16;  // Anderson generations (the system and th fit in sdot)
+__device__ bool small_solve(int n, double *A, double *r) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i * n + k]) > fabs(A[p * n + k])) p = i;
+    if (A[p * n + k] == 0.0 || !isfinite(A[p * n + k])) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) {
+        const double t = A[k * n + j];
+        A[k * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
+      const double t = r[k];
+      r[k] = r[p];
+      r[p] = t;
+    }
+    const double inv = 1.0 / A[k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      const double f = A[i * n + k] * inv;
+      for (int j = k; j < n; ++j) A[i * n + j] = fma(-f, A[k * n + j], A[i * n + j]);
+      r[i] = fma(-f, r[k], r[i]);
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double v = r[k];
+    for (int j = k + 1; j < n; ++j) v = fma(-A[k * n + j], r[j], v);
+    r[k] = v / A[k * n + k];
+  }
+  return true;
+}
+
+// One step of the reference's full-mode SCF loop with its Anderson mixer
+// (scf/unrolling/default.py:80-140 with mix_guess; scf/mixer/anderson.py:
+// 163-317, after Eyert): F = G(x) - x; convergence when |F|_2 < x_atol and
+// max |F| < x_atol_max (mixer/base.py:230-256), checked from the second call
+// on (the first mixes the guess); then the converged value is G(x), and one
+// more pass evaluates the energy there (scf/base.py converged_to_charges).
+// Mixing: simple x + damp_init F for the first `generations` calls (soft
+// start) or the first call, else x_bar + damp F_bar with the coefficients th
+// of (dF_i . dF_j)(1 + offset^2 on the diagonal) th = dF_i . F, dF_i = F -
+// F_i over the last min(call - 1, generations) entries. The histories X (in
+// hx) and F (in hr) are rings of generations + 1 vectors. Lead CTA only.
+__device__ int anderson_step(const ScfArgs &a, Ws &w, int N, int it, Broyden &br, int &status,
+                             double *red) {
+  const int G = a.generations, H = G + 1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (int)(blockDim.x >> 5);
+  auto X = [&](int h) { return w.hx + (size_t)((br.base + h) % H) * N; };
+  auto F = [&](int h) { return w.hr + (size_t)((br.base + h) % H) * N; };
+  double *x0 = X(0), *f0 = F(0);
+  double p2 = 0.0, pm = 0.0;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    const double xt = w.x[t], ft = w.g[t] - xt;
+    x0[t] = xt;
+    f0[t] = ft;
+    p2 = fma(ft, ft, p2);
+    pm = fmax(pm, fabs(ft));
+  }
+  const double l2 = sqrt(block_sum(p2, red));
+  const double mx = block_max(pm, red);
+  br.resid = l2;
+  if (!isfinite(l2)) {
+    status = DXTB_ERR_NAN;
+    return kStop;
+  }
+  // the loop ends after maxiter calls beyond the guess-mixing one
+  const bool conv = it >= 2 && l2 < a.xtol && mx < a.xtol_max;
+  if (conv || it >= a.maxiter + 1) {
+    for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = w.g[t];
+    br.final_eval = 1;
+    br.hit_max = conv ? 0 : 1;
+    __syncthreads();
+    return kNext;
+  }
+  double *sdot = w.sdot;  // [0, n(n+1)/2 + n): the system; then th
+  if (it > G || (it > 1 && !a.soft_start)) {
+    const int n = min(it - 1, G);
+    const int npair = n * (n + 1) / 2;
+    // task k < npair: (dF_i . dF_j), i <= j; then dF_i . F
+    for (int k = wid; k < npair + n; k += nw) {
+      int i, j;
+      if (k < npair) {
+        i = 0;
+        while ((i + 1) * (i + 2) / 2 <= k) ++i;
+        j = k - i * (i + 1) / 2;  // j <= i
+      } else {
+        i = k - npair;
+        j = -1;
+      }
+      const double *fi = F(i + 1), *fj = j >= 0 ? F(j + 1) : nullptr;
+      double s = 0.0;
+      for (int t = lane; t < N; t += 32) {
+        const double di = f0[t] - fi[t];
+        s = fma(di, j >= 0 ? f0[t] - fj[t] : f0[t], s);
+      }
+      s = warp_sum(s);
+      if (lane == 0) sdot[k] = s;
+    }
+    __syncthreads();
+    double *A = sdot + npair + n, *th = A + n * n;
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j <= i; ++j) {
+          const double v = sdot[i * (i + 1) / 2 + j];
+          A[i * n + j] = v;
+          A[j * n + i] = v;
+        }
+        A[i * n + i] *= 1.0 + a.offset * a.offset;
+        th[i] = sdot[npair + i];
+      }
+      w.team[48] = small_solve(n, A, th) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (w.team[48] == 0.0) {
+      status = DXTB_ERR_NAN;
+      return kStop;
+    }
+    // x_mix = X0 + damp F0 + sum_i th_i ((X_i - X0) + damp (F_i - F0))
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      const double xt = x0[t], ft = f0[t];
+      double v = fma(a.damp, ft, xt);
+      for (int i = 0; i < n; ++i) v = fma(th[i], (X(i + 1)[t] - xt) + a.damp * (F(i + 1)[t] - ft), v);
+      w.x[t] = v;
+    }
+  } else {
+    for (int t = threadIdx.x; t < N; t += blockDim.x) w.x[t] = fma(a.damp_init, f0[t], x0[t]);
+  }
+  br.base = (br.base + H - 1) % H;  // entry 0 of this call becomes entry 1
+  __syncthreads();
   return kNext;
 }
 
@@ -610,8 +750,9 @@ __device__ void scf_body(const ScfArgs &a, int m_, Team<CL> &tm, double *dsm, bo
       potential_from_charges<CL>(a, mv, qo, dpa, qpa, qsh, qat, vsh, vat, w.g, multipole, es3_shell);
       int act;
       if (br.final_eval) {
-        br.hit_max = 1;
-        act = kStop;
+        act = kStop;  // hit_max as set when the final evaluation was scheduled
+      } else if (a.mixer == DXTB_MIXER_ANDERSON) {
+        act = anderson_step(a, w, N, it, br, status, red);
       } else {
         act = broyden_step(a, w, N, it, br, status, red);
       }
@@ -953,12 +1094,38 @@ extern "C" int32_t dxtb_scf_set_size_classes(const int32_t *min_n) {
   return DXTB_OK;
 }
 
+namespace dxtb {
+
+// Checks a configuration and copies it into the kernel arguments.
+static int32_t apply_config(const dxtb_scf_config *c, ScfArgs &a) {
+  if (!c || c->maxiter <= 0 || !(c->x_atol > 0.0) || !(c->f_atol > 0.0) || !(c->damp > 0.0))
+    return DXTB_ERR_ARGS;
+  if (c->mixer != DXTB_MIXER_BROYDEN1 && c->mixer != DXTB_MIXER_ANDERSON) return DXTB_ERR_ARGS;
+  if (c->mixer == DXTB_MIXER_ANDERSON &&
+      (c->generations < 1 || c->generations > kMaxGen || !(c->x_atol_max > 0.0) || !(c->damp_init > 0.0) ||
+       !(c->diagonal_offset >= 0.0)))
+    return DXTB_ERR_ARGS;
+  a.maxiter = c->maxiter;
+  a.mixer = c->mixer;
+  a.xtol = c->x_atol;
+  a.ftol = c->f_atol;
+  a.xtol_max = c->x_atol_max;
+  a.damp = c->damp;
+  a.damp_init = c->damp_init;
+  a.generations = c->generations;
+  a.soft_start = c->soft_start;
+  a.offset = c->diagonal_offset;
+  return DXTB_OK;
+}
+
+}  // namespace dxtb
+
 extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                             const double *overlap, const double *h0, const double *dipole,
                             const double *quadrupole, const double *gamma, const double *hd,
                             const double *amat_sd, const double *amat_dd, const double *amat_sq,
                             const double *gb_mat, const double *n0, const double *nel, double kt,
-                            int32_t maxiter, double tol, const int64_t *ws_off,
+                            const dxtb_scf_config *cfg, const int64_t *ws_off,
                             const int32_t *order, double *workspace, double *density,
                             double *wdensity, double *coeff, double *evals, double *occ, double *q,
                             double *dp, double *qp, double *vorb, double *vdp, double *vqp,
@@ -966,8 +1133,9 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   if (!b || b->nmol <= 0 || !overlap || !h0 || !gamma || !hd || !n0 || !nel || !ws_off ||
       !workspace || !density || !coeff || !evals || !occ || !q || !vorb || !energies || !status)
     return DXTB_ERR_ARGS;
-  if (maxiter <= 0 || !(kt > 0.0)) return DXTB_ERR_ARGS;
+  if (!(kt > 0.0)) return DXTB_ERR_ARGS;
   ScfArgs a;
+  if (apply_config(cfg, a) != DXTB_OK) return DXTB_ERR_ARGS;
   a.b = *b;
   a.pf = par_f;
   a.pi = par_i;
@@ -984,9 +1152,6 @@ extern "C" int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int3
   a.n0 = n0;
   a.nel = nel;
   a.kt = kt;
-  a.xtol = tol;  // x_atol and f_atol of the reference: one tolerance here
-  a.ftol = tol;
-  a.maxiter = maxiter;
   a.ws_off = ws_off;
   a.order = order;
   a.ws = workspace;
@@ -1010,7 +1175,7 @@ extern "C" int32_t dxtb_scf_gradient(
     const dxtb_batch *b, const double *par_f, const int32_t *par_i, const double *overlap,
     const double *h0, const double *dipole, const double *quadrupole, const double *gamma,
     const double *hd, const double *amat_sd, const double *amat_dd, const double *amat_sq,
-    const double *gb_mat, const double *n0, const double *nel, double kt, int32_t maxiter, double tol,
+    const double *gb_mat, const double *n0, const double *nel, double kt, const dxtb_scf_config *cfg,
     const int64_t *ws_off, const int32_t *order, double *workspace, double *density,
     double *wdensity, double *coeff, double *evals, double *occ, double *q, double *dp, double *qp,
     double *vorb, double *vdp, double *vqp, double *energies, int32_t *status, const double *cn,
@@ -1019,9 +1184,10 @@ extern "C" int32_t dxtb_scf_gradient(
       !workspace || !density || !wdensity || !coeff || !evals || !occ || !q || !vorb || !energies ||
       !status || !cn || !dedcn || !grad)
     return DXTB_ERR_ARGS;
-  if (maxiter <= 0 || !(kt > 0.0)) return DXTB_ERR_ARGS;
+  if (!(kt > 0.0)) return DXTB_ERR_ARGS;
   if (dipole != nullptr && (!vdp || !vqp || !dp || !qp || !mrad)) return DXTB_ERR_ARGS;
   ScfArgs a;
+  if (apply_config(cfg, a) != DXTB_OK) return DXTB_ERR_ARGS;
   a.b = *b;
   a.pf = par_f;
   a.pi = par_i;
@@ -1038,9 +1204,6 @@ extern "C" int32_t dxtb_scf_gradient(
   a.n0 = n0;
   a.nel = nel;
   a.kt = kt;
-  a.xtol = tol;
-  a.ftol = tol;
-  a.maxiter = maxiter;
   a.ws_off = ws_off;
   a.order = order;
   a.ws = workspace;
@@ -1145,8 +1308,15 @@ extern "C" int32_t dxtb_scf_noalloc(
     return DXTB_ERR_LAUNCH;
   if (cudaStreamSynchronize(st) != cudaSuccess) return DXTB_ERR_LAUNCH;
   if (need > DXTB_NOALLOC_SCRATCH_DOUBLES) return DXTB_ERR_TOO_LARGE;
+  // the implicit-mode root solver with one tolerance for x_atol and f_atol
+  dxtb_scf_config cfg = {};
+  cfg.maxiter = maxiter;
+  cfg.mixer = DXTB_MIXER_BROYDEN1;
+  cfg.x_atol = tol;
+  cfg.f_atol = tol;
+  cfg.damp = 0.5;
   return dxtb_scf(b, par_f, par_i, overlap, h0, dipole, quadrupole, gamma, hd, amat_sd, amat_dd,
-                  amat_sq, gb_mat, n0, nel, kt, maxiter, tol, hdr + kNoallocHeader, order,
+                  amat_sq, gb_mat, n0, nel, kt, &cfg, hdr + kNoallocHeader, order,
                   scratch + ws_start, density, wdensity, coeff, evals, occ, q, dp, qp, vorb, vdp,
                   vqp, energies, status, stream);
 }

@@ -209,13 +209,39 @@ def gb_args(gb: dict) -> tuple:
             float(gb.get("born_scale", 1.0)), float(gb.get("born_offset", 0.0)))
 
 
+SCF_DEFAULTS = {
+    # the reference's ConfigSCF defaults (constants/defaults.py) for the
+    # full-mode mixer; the implicit-mode broyden1 uses damp only
+    "damp": 0.5, "damp_init": 0.1, "generations": 5, "soft_start": True,
+    "diagonal_offset": 0.01, "x_atol_max": 1e-5,
+}
+
+
+def scf_config(maxiter: int, tol: float, scf: dict | None = None) -> _lib.ScfConfig:
+    """The C configuration of the SCF. ``scf`` may set ``mixer``
+    ("broyden1": implicit mode, "anderson": full mode), ``x_atol``, ``f_atol``,
+    ``x_atol_max``, ``damp``, ``damp_init``, ``generations``, ``soft_start``
+    and ``diagonal_offset``; ``tol`` is the default of x_atol and f_atol."""
+    o = dict(SCF_DEFAULTS)
+    o.update(scf or {})
+    mixer = o.get("mixer", "broyden1")
+    if mixer not in _lib.MIXERS:
+        raise ValueError(f"unknown SCF mixer {mixer!r}")
+    return _lib.ScfConfig(
+        int(maxiter), _lib.MIXERS[mixer], float(o.get("x_atol", tol)), float(o.get("f_atol", tol)),
+        float(o["x_atol_max"]), float(o["damp"]), float(o["damp_init"]), int(o["generations"]),
+        1 if o["soft_start"] else 0, float(o["diagonal_offset"]),
+    )
+
+
 def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float = 1e-10,
         forces: bool = False, gb: dict | None = None, state: dict | None = None,
-        events: dict | None = None) -> Result:
+        events: dict | None = None, scf: dict | None = None) -> Result:
     """
     One single point for every molecule of the packed batch. With ``events``
     (a dict), CUDA events are recorded on the current stream around each
-    stage: events[stage] = (start, end).
+    stage: events[stage] = (start, end). ``scf`` selects the root solver
+    and its tolerances (``scf_config``).
     """
     L = _lib.lib()
 
@@ -300,9 +326,10 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
         s["status"] = status
     ws = buf("ws", tot["ws"])
     kt = etemp * radii.KELVIN2AU
+    cfg = scf_config(maxiter, tol, scf)
     scf_args = (b, pf, pi, S.data_ptr(), H.data_ptr(), _lib.ptr(D), _lib.ptr(Q), gamma.data_ptr(),
                 hd.data_ptr(), _lib.ptr(sd), _lib.ptr(dd), _lib.ptr(sq), _lib.ptr(gbm),
-                pb.t["n0"].data_ptr(), pb.t["nel"].data_ptr(), kt, int(maxiter), float(tol),
+                pb.t["n0"].data_ptr(), pb.t["nel"].data_ptr(), kt, C.byref(cfg),
                 pb.t["ws_off"].data_ptr(), pb.t["order"].data_ptr(), ws.data_ptr(), P.data_ptr(),
                 _lib.ptr(W), Cm.data_ptr(), ev.data_ptr(), occ.data_ptr(), q.data_ptr(),
                 dp.data_ptr(), qp.data_ptr(), vorb.data_ptr(), vdp.data_ptr(), vqp.data_ptr(),

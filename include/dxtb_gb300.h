@@ -194,6 +194,34 @@ int32_t dxtb_multipole_raw(const dxtb_batch *b, const double *par_f,
                            const int32_t *par_i, double *overlap,
                            double *dipole, double *quadrupole, void *stream);
 
+/* ---- SCF configuration (calculators/config/scf.py ConfigSCF) -----------
+ * mixer DXTB_MIXER_BROYDEN1: the implicit-mode root solver (scf_mode
+ * "implicit": xitorch broyden1 on F(x) = x - G(x), exlibs/xitorch/_impls/
+ * optimize/root/rootsolver.py:42-265 with alpha = -0.5 and damp), stopping
+ * when |dx|_2 < x_atol and |F|_2 < f_atol, returning the best iterate after
+ * maxiter iterations. DXTB_MIXER_ANDERSON: the full-mode loop (scf_mode
+ * "full", scf/unrolling/default.py:71-140, mix_guess) with the Anderson
+ * mixer of scf/mixer/anderson.py:163-317 (damp, damp_init, generations
+ * <= 16, soft_start, diagonal_offset), converged when |G(x) - x|_2 < x_atol
+ * and max |G(x) - x| < x_atol_max (scf/mixer/base.py:230-256), the energy
+ * evaluated at G(x). Reference defaults (constants/defaults.py): maxiter
+ * 100, x_atol = f_atol = 1e-4, x_atol_max = 1e-5, damp 0.5, damp_init 0.1,
+ * generations 5, soft_start 1, diagonal_offset 0.01. */
+#define DXTB_MIXER_BROYDEN1 0
+#define DXTB_MIXER_ANDERSON 1
+typedef struct dxtb_scf_config {
+  int32_t maxiter;
+  int32_t mixer;
+  double x_atol;
+  double f_atol;
+  double x_atol_max;
+  double damp;
+  double damp_init;
+  int32_t generations;
+  int32_t soft_start;
+  double diagonal_offset;
+} dxtb_scf_config;
+
 /* SCF workspace of one molecule in doubles (n AOs, nat atoms); the caller
  * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
 int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
@@ -204,9 +232,9 @@ int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);
  * wavefunction/filling.py:428-742, exlibs/xitorch symeig): Fock build,
  * generalized eigensolve, Fermi occupations at kT, density, Mulliken
  * charges and multipole moments, potentials, and the limited-memory
- * Broyden root solve of x - G(x) on the potential (xitorch broyden1,
- * exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265); per-molecule
- * convergence |dx|_2 < tol and |x - G(x)|_2 < tol, iteration cap.
+ * root solve of x - G(x) on the potential configured by cfg (the
+ * implicit-mode broyden1 or the full-mode Anderson mixer, see
+ * dxtb_scf_config) with per-molecule convergence and iteration cap.
  * order: [nmol] launch order (largest first) or null. Inputs are the
  * integrals and caches of the calls above, n0 [naos] reference occupation,
  * nel [nmol][2] alpha/beta electrons, gb_mat [nat2] or null. Outputs:
@@ -222,7 +250,7 @@ int32_t dxtb_scf(const dxtb_batch *b, const double *par_f, const int32_t *par_i,
                  const double *quadrupole, const double *gamma,
                  const double *hd, const double *amat_sd, const double *amat_dd,
                  const double *amat_sq, const double *gb_mat, const double *n0,
-                 const double *nel, double kt, int32_t maxiter, double tol,
+                 const double *nel, double kt, const dxtb_scf_config *cfg,
                  const int64_t *ws_off, const int32_t *order,
                  double *workspace, double *density, double *wdensity,
                  double *coeff, double *evals, double *occ, double *q,
@@ -257,7 +285,7 @@ int32_t dxtb_scf_gradient(const dxtb_batch *b, const double *par_f,
                           const double *hd, const double *amat_sd,
                           const double *amat_dd, const double *amat_sq,
                           const double *gb_mat, const double *n0,
-                          const double *nel, double kt, int32_t maxiter, double tol,
+                          const double *nel, double kt, const dxtb_scf_config *cfg,
                           const int64_t *ws_off, const int32_t *order,
                           double *workspace, double *density, double *wdensity,
                           double *coeff, double *evals, double *occ, double *q,

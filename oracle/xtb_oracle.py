@@ -851,13 +851,19 @@ def singlepoint(
     grad: bool = False,
     exclude: tuple = (),
     mixer: str = "broyden1",
+    anderson: dict | None = None,
 ) -> Result:
     """
-    GFN1/GFN2 single point: SCF on the potential to ``tol`` (the converged
-    point of ``scf/implicit`` with Broyden), energy as in
+    GFN1/GFN2 single point: SCF on the potential, energy as in
     ``scf/base.py:510-619`` + repulsion; with ``grad`` the forces are
-    ``-dE/dR`` from autograd of the energy functional at the converged density
+    ``-dE/dR`` from autograd of the energy functional at the final density
     (variational: ``E[P, R] - tr(W S(R))``).
+
+    mixer "broyden1": the implicit mode's root solver to ``tol`` (x_atol =
+    f_atol), ``broyden1_loop``. mixer "anderson": the full mode's loop with
+    the Anderson mixer, ``anderson_loop``, with the options of ``anderson``
+    (reference defaults: x_atol 1e-4, x_atol_max 1e-5, damp 0.5, damp_init
+    0.1, generations 5, soft_start, diagonal_offset 0.01) and ``maxiter``.
     """
     sysm = make_system(method, numbers)
     pos = torch.as_tensor(positions, dtype=DT).clone()
@@ -888,89 +894,11 @@ def singlepoint(
             return torch.cat(parts), (p, cmat, ev, fa, fb, qo, dp, qp)
 
         x = torch.zeros(sysm.nao + (9 * nat if d is not None else 0), dtype=DT)
-        # Anderson mixing on the potential (or modified Broyden, mixer="broyden")
-        hist_x, hist_f = [], []
-        dfs, us, r_old, x_old = [], [], None, None
-        it = 0
-        for it in range(1, maxiter + 1):
-            gx, aux = f_map(x)
-            r = gx - x
-            if mixer != "broyden1" and float(r.abs().max()) < tol:
-                x = gx
-                break
-            if mixer == "broyden1":
-                # exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265 and
-                # _jacobian.py:51-120 with alpha=-0.5, damp=0.5, no line search
-                # (scf/base.py:267-292); F(x) = x - G(x), Gm = 0.5 I + C D^T
-                y = -r
-                ynorm = float(torch.linalg.norm(y))
-                if it == 1:
-                    cs, ds = [], []
-                    best = (ynorm, x.clone())
-                else:
-                    if ynorm < best[0]:
-                        best = (ynorm, x.clone())
-                    dxx, dyy = x - x_old, y - y_old
-
-                    def gm(v):
-                        out = 0.5 * v
-                        for c_, d_ in zip(cs, ds):
-                            out = out + c_ * torch.dot(d_, v)
-                        return out
-
-                    def gmt(v):
-                        out = 0.5 * v
-                        for c_, d_ in zip(cs, ds):
-                            out = out + d_ * torch.dot(c_, v)
-                        return out
-
-                    v = gmt(dxx)
-                    c_new = dxx - gm(dyy)
-                    d_new = v / torch.dot(dyy, v)
-                    cs.append(c_new)
-                    ds.append(d_new)
-                    if dx_norm < tol and ynorm < tol:
-                        break
-                if it == maxiter:
-                    x = best[1]
-                    break
-                dxv = -0.5 * y
-                for c_, d_ in zip(cs, ds):
-                    dxv = dxv - c_ * torch.dot(d_, y)
-                dx_norm = float(torch.linalg.norm(dxv))
-                x_old, y_old = x.clone(), y.clone()
-                x = x + 0.5 * dxv
-                continue
-            if mixer == "broyden":
-                if r_old is not None:
-                    dfr = r - r_old
-                    nrm = torch.linalg.norm(dfr)
-                    dfs.append(dfr / nrm)
-                    us.append(0.2 * dfr / nrm + (x - x_old) / nrm)
-                    if len(dfs) > 16:
-                        dfs.pop(0)
-                        us.pop(0)
-                x_old, r_old = x.clone(), r.clone()
-                if dfs:
-                    F, U = torch.stack(dfs, 1), torch.stack(us, 1)
-                    a = F.T @ F + 1e-4 * torch.eye(len(dfs), dtype=DT)
-                    x = x + 0.2 * r - U @ torch.linalg.solve(a, F.T @ r)
-                else:
-                    x = x + 0.2 * r
-                continue
-            hist_x.append(x.clone())
-            hist_f.append(r.clone())
-            if len(hist_x) > 8:
-                hist_x.pop(0)
-                hist_f.pop(0)
-            m = len(hist_f)
-            if m == 1:
-                x = x + 0.4 * r
-            else:
-                df = torch.stack([hist_f[i + 1] - hist_f[i] for i in range(m - 1)], 1)
-                dx = torch.stack([hist_x[i + 1] - hist_x[i] for i in range(m - 1)], 1)
-                gam = torch.linalg.lstsq(df, r[:, None]).solution[:, 0]
-                x = x + 0.4 * r - (dx + 0.4 * df) @ gam
+        if mixer == "anderson":
+            x, it, conv = anderson_loop(lambda v: f_map(v)[0], x, maxiter, anderson or {})
+            hit_max = not conv
+        else:
+            x, it, hit_max = broyden1_loop(lambda v: f_map(v)[0], x, maxiter, tol)
         gx, aux = f_map(x)
         p, cmat, ev, fa, fb, qo, dp, qp = aux
         occ = fa + fb
@@ -986,7 +914,7 @@ def singlepoint(
         e_rep = repulsion_energy(sysm, pos) if "rep" not in exclude else torch.zeros((), dtype=DT)
         w = (cmat * (occ * ev)) @ cmat.T
     energy = float(e_h0 + e_int + e_free + e_rep)
-    extra = {"e_h0": float(e_h0), "e_int": float(e_int), "s": s, "h0": h0}
+    extra = {"e_h0": float(e_h0), "e_int": float(e_int), "s": s, "h0": h0, "converged": not hit_max}
     res = Result(
         energy, float(e_h0 + e_int), float(e_rep), float(e_free), it, p, w, qo,
         ev, occ, cn, extra,
@@ -994,6 +922,113 @@ def singlepoint(
     if grad:
         res.extra["gradient"] = gradient(sysm, pos, p, w, n0, solvation, exclude)
     return res
+
+
+def broyden1_loop(g_map, x, maxiter: int, tol: float, alpha: float = -0.5, damp: float = 0.5):
+    """
+    The implicit mode's root solver on F(x) = x - G(x): xitorch broyden1
+    (exlibs/xitorch/_impls/optimize/root/rootsolver.py:42-265 and
+    _jacobian.py:51-120 with alpha = -0.5, damp = 0.5, no line search;
+    scf/base.py:267-292), inverse Jacobian Gm = -alpha I + C D^T, stop when
+    |dx|_2 < tol and |F|_2 < tol; after maxiter the best iterate is returned.
+    Returns (x, iterations, hit_maxiter).
+    """
+    cs, ds = [], []
+    best = None
+    x_old = y_old = None
+    dx_norm = float("inf")
+    it = 0
+    for it in range(1, maxiter + 1):
+        y = x - g_map(x)
+        ynorm = float(torch.linalg.norm(y))
+        if it == 1:
+            best = (ynorm, x.clone())
+        else:
+            if ynorm < best[0]:
+                best = (ynorm, x.clone())
+            dxx, dyy = x - x_old, y - y_old
+
+            def gm(v):
+                out = -alpha * v
+                for c_, d_ in zip(cs, ds):
+                    out = out + c_ * torch.dot(d_, v)
+                return out
+
+            def gmt(v):
+                out = -alpha * v
+                for c_, d_ in zip(cs, ds):
+                    out = out + d_ * torch.dot(c_, v)
+                return out
+
+            v = gmt(dxx)
+            cs.append(dxx - gm(dyy))
+            ds.append(v / torch.dot(dyy, v))
+            if dx_norm < tol and ynorm < tol:
+                return x, it, False
+        if it == maxiter:
+            return best[1], it, True
+        dxv = alpha * y
+        for c_, d_ in zip(cs, ds):
+            dxv = dxv - c_ * torch.dot(d_, y)
+        dx_norm = float(torch.linalg.norm(dxv))
+        x_old, y_old = x.clone(), y.clone()
+        x = x + damp * dxv
+    return x, it, True
+
+
+def anderson_loop(g_map, guess, maxiter: int, opts: dict):
+    """
+    The full mode's SCF loop (scf/unrolling/default.py:80-140: mix_guess,
+    then up to maxiter calls, convergence tested after each mixing on the
+    current difference) with the Anderson mixer (scf/mixer/anderson.py:
+    163-317, Eyert's method without theta_0; mixer/base.py:230-256 for the
+    convergence test |F|_2 < x_atol and max|F| < x_atol_max). Returns
+    (G(x) at the last call, loop iterations, converged): the reference
+    evaluates the energy at that converged value (converged_to_charges).
+    """
+    damp = opts.get("damp", 0.5)
+    damp_init = opts.get("damp_init", 0.1)
+    gens = opts.get("generations", 5)
+    offset = opts.get("diagonal_offset", 0.01)
+    soft = opts.get("soft_start", True)
+    x_tol = opts.get("x_atol", 1e-4)
+    x_tol_max = opts.get("x_atol_max", 1e-5)
+    xh = torch.zeros(gens + 1, len(guess), dtype=DT)  # x history, entry 0 = current input
+    fh = torch.zeros(gens + 1, len(guess), dtype=DT)  # difference history
+    step = 0
+
+    def mix(x_new, x_old):
+        nonlocal step, xh, fh
+        xh[0] = x_old
+        step += 1
+        fh[0] = x_new - x_old
+        if step > gens or (step > 1 and not soft):
+            n = min(step - 1, gens)
+            df = fh[0] - fh[1 : n + 1]
+            a = df @ df.T
+            b = df @ fh[0]
+            eye = torch.eye(n, dtype=DT)
+            a = a * torch.where(eye != 0, eye + offset**2, torch.ones((), dtype=DT))
+            th = torch.linalg.solve(a, b)
+            x_bar = th @ (xh[1 : n + 1] - xh[0]) + xh[0]
+            f_bar = th @ (-df) + fh[0]
+            x_mix = x_bar + damp * f_bar
+        else:
+            x_mix = xh[0] + damp_init * fh[0]
+        delta = fh[0].clone()
+        fh = torch.roll(fh, 1, 0)
+        xh = torch.roll(xh, 1, 0)
+        xh[0] = x_mix
+        return x_mix, delta
+
+    q_new = g_map(guess)
+    q, _ = mix(q_new, guess)
+    for it in range(1, maxiter + 1):
+        q_new = g_map(q)
+        q, delta = mix(q_new, q)
+        if float(torch.linalg.norm(delta)) < x_tol and float(delta.abs().max()) < x_tol_max:
+            return q_new, it, True
+    return q_new, maxiter, False
 
 
 def gradient(sysm: System, positions, p, w, n0, solvation=None, exclude=()) -> torch.Tensor:

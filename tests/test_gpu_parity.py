@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 E_TOL = 1e-8   # Eh
 F_TOL = 1e-6   # Eh/Bohr
 G = np.load(__import__("pathlib").Path(__file__).parent / "golden" / "golden.npz")
-OPTS = {"exclude": ["disp", "d4sc", "hal"]}
+# implicit-mode SCF converged to 1e-10 (x_atol = f_atol), zero-potential start
+OPTS = {"exclude": ["disp", "d4sc", "hal"], "scf_mode": "implicit", "x_atol": 1e-10,
+        "f_atol": 1e-10, "maxiter": 250, "guess": "sad"}
 
 
 def calc(method, numbers):
@@ -185,3 +187,33 @@ def test_config3_adjoint_forces_vs_oracle_and_fd(method):
             pbi = PackedBatch(tables(method), [num], [torch.tensor(q)])
             e.append(float(run(pbi).energy[0]))
         assert abs((e[0] - e[1]) / (2 * h) - g0[a, x]) < F_TOL
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_reference_default_options(method):
+    """A calculator with the reference's default SCF options (full mode, whose
+    Broyden setting falls back to Anderson; maxiter 100; x_atol 1e-4,
+    x_atol_max 1e-5) against the oracle's restatement of that loop: the same
+    trajectory, so energies agree to 1e-8, and the forces (the variational
+    gradient at the final density on both sides) to 1e-6."""
+    import warnings
+
+    from dxtb_gb300 import GFN1Calculator, GFN2Calculator
+    from dxtb_gb300.workloads import random_molecule
+
+    num, pos = random_molecule(2100 + (method == "gfn2"), 24)
+    cls = GFN1Calculator if method == "gfn1" else GFN2Calculator
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        c = cls(torch.as_tensor(num), opts={"exclude": ["disp", "d4sc", "hal"]}, device="cuda")
+    msgs = " ".join(str(x.message) for x in w)
+    assert "Anderson" in msgs and "EEQ" in msgs
+    p = torch.tensor(pos, device="cuda")
+    e = float(c.get_energy(p))
+    f = c.get_forces(p).cpu().numpy()
+    ref = X.singlepoint(method, num, pos, grad=True, mixer="anderson", maxiter=100)
+    assert ref.extra["converged"]
+    res = c.singlepoint(p)
+    assert int(res.iter[0]) == ref.iterations + 2  # guess-mixing pass and the final evaluation
+    assert abs(e - ref.energy) < E_TOL
+    assert np.abs(f + ref.extra["gradient"].numpy()).max() < F_TOL

@@ -63,12 +63,13 @@ def test_gfn1_alpb_mb16_43_01_energy_and_gradient():
 
     z = torch.tensor(G["MB16_43_01/numbers"])
     pos = torch.tensor(G["MB16_43_01/positions"], device="cuda")
-    opts = {"exclude": ["disp", "hal"]}
+    opts = {"exclude": ["disp", "hal"], "scf_mode": "implicit", "x_atol": 1e-10, "f_atol": 1e-10,
+            "maxiter": 250, "guess": "sad"}
     vac = GFN1Calculator(z, opts=opts, device="cuda").singlepoint(pos)
     gb = GeneralizedBorn(z, 78.9)
     calc = GFN1Calculator(z, interaction=[gb], opts=opts, device="cuda")
     sol = calc.singlepoint(pos)
-    gsolv = float(sol["scf"] - vac["scf"])
+    gsolv = float(sol.scf - vac.scf)
     assert abs(gsolv - G["solv/MB16_43_01/gsolv"].sum()) < 1e-7
     ref = X.singlepoint("gfn1", z.numpy(), pos.cpu().numpy(), tol=1e-12, solvation={"epsilon": 78.9},
                         grad=True)
