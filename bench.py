@@ -53,6 +53,9 @@ def args():
     p.add_argument("--serve-rate", type=float, default=2000.0,
                    help="Poisson arrival rate of the serving leg (0: skip the leg)")
     p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--config4", action="store_true",
+                   help="also run the serving configuration: 200 Poisson requests at 2000/s, "
+                        "GFN1/GFN2, 8-300 atoms log-uniform, E+F, 120 GB budget")
     return p.parse_args()
 
 
@@ -309,6 +312,9 @@ def main():
     pb = PackedBatch(tables("gfn2"), nums, pos, dev)
     state: dict = {}
     l2 = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    from dxtb_gb300 import autotune
+
+    tuned = autotune.ensure(pb)  # size-class policy: cached, or tuned once on this batch
     for _ in range(a.warmup):
         res = run(pb, forces=True, state=state)
     torch.cuda.synchronize()
@@ -422,6 +428,31 @@ def main():
                         "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
                         "hbm_budget_gb": 120.0, "status_bad": sum(1 for r in out if r.status != 0)})
 
+    # the serving configuration (8-300 atoms, both methods) through the two-lane loop
+    config4 = None
+    if a.config4:
+        from dxtb_gb300.serving import (CudaExecutor, Server, latency_summary, poisson_requests,
+                                        warm_up)
+
+        reqs = poisson_requests(200, 2000.0, 4)
+        slots, large_slots = 8, 3
+        ex = CudaExecutor(dev, slots=slots, priorities=[-100] * (slots - large_slots) + [0] * large_slots)
+        warm_up(ex, slots)
+        torch.cuda.synchronize()
+        srv = Server(ex, hbm_budget=120e9, slots=slots, max_pack=32, large_slots=large_slots,
+                     large_n=320, large_pack=4, order="size")
+        out = srv.serve(reqs)
+        config4 = latency_summary(out)
+        config4.update({
+            "workload": "200 requests, Poisson 2000/s (seed 4), GFN1/GFN2, 8-300 atoms log-uniform, E+F",
+            "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
+            "max_bytes_gb": srv.stats.max_bytes / 1e9, "hbm_budget_gb": 120.0,
+            "iterations_max": int(max(r.iterations for r in out)),
+            "status_bad": [[int(r.rid), int(r.status), int(r.iterations)] for r in out if r.status != 0],
+            "slowest": sorted([[int(r.rid), round(r.latency_ms, 1), int(r.iterations)] for r in out],
+                              key=lambda v: -v[1])[:5],
+        })
+
     cpu_baseline = None
     if rank == 0 and a.cpu_sample > 0:
         cpu_baseline, ref_e = cpu_reference(mols, a.cpu_sample)
@@ -479,9 +510,11 @@ def main():
                           "peak_gbs": hbm_peak, "frac": int_gbs / hbm_peak if hbm_peak else None},
         },
         "fp64_probes_tflops": peaks,
+        "autotune": tuned,
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
         "serving": serving,
+        "config4": config4,
         "gpu_launches": res.launches * a.steps,
         "clocks": clk,
     }

@@ -14,9 +14,10 @@ H0, interactions, the SCF and the analytic gradient. The energy is a
 adjoint kernels, so ``energy.backward()`` and ``torch.autograd.grad`` work on
 the positions as in the reference.
 
-Not computed (the reference's defaults include them): D3/D4 dispersion and
-the GFN1 halogen-bond term; callers wanting parity pass
-``opts={"exclude": ["disp", "hal"]}`` to the reference.
+Not computed (the reference's defaults include it): D3/D4 dispersion;
+callers wanting parity pass ``opts={"exclude": ["disp", "d4sc"]}`` to the
+reference. The GFN1 halogen-bond term is zero for every accepted element
+(its bond strengths are nonzero only for Br, I and At).
 
 SCF options follow the reference's ConfigSCF (constants/defaults.py):
 ``scf_mode`` "full" (default; the loop of scf/unrolling with the Anderson
@@ -166,10 +167,14 @@ class Calculator:
                 else:
                     raise NotImplementedError(f"interaction {type(it).__name__} is not on the GB300 path")
         excl = set(self.opts.get("exclude", []))
-        if not {"disp", "d4sc"}.issubset(excl) or (self.method == "gfn1" and "hal" not in excl):
+        # The GFN1 halogen-bond term (components/classicals/halogen/hal.py)
+        # needs a halogen with a bond strength: xbond is nonzero only for Br,
+        # I and At, outside the elements this path accepts (H-Ar), so it is
+        # exactly zero here, as in the reference.
+        if "disp" not in excl or (self.method == "gfn2" and "d4sc" not in excl):
             warnings.warn(
-                "dispersion (and GFN1 halogen bonding) is not part of the GB300 path; "
-                "results equal the reference with exclude=['disp', 'd4sc', 'hal']",
+                "dispersion is not part of the GB300 path; results equal the reference "
+                "with exclude=['disp', 'd4sc']",
                 stacklevel=2,
             )
         self.include_rep = "rep" not in excl
@@ -294,6 +299,9 @@ class Calculator:
             self._pb = engine.PackedBatch(self.tables, self._mols, plist, self.device, chg,
                                           [int(s) for s in spins] if spins else None)
             self._pb_key = key
+            from . import autotune
+
+            autotune.ensure(self._pb)  # large batches: the tuned size-class policy
         else:
             self._pb.set_positions(plist)
         res = engine.run(self._pb, etemp=self.etemp, maxiter=self.maxiter, tol=self.tol,
@@ -344,6 +352,31 @@ class Calculator:
     def forces(self, positions, chrg=0, spin=None):
         r = self._run(positions.detach(), chrg, spin, forces=True)
         return -r["gradient"]
+
+    def hessian(self, positions, chrg=0, spin=None, use_functorch=False,
+                derived_quantity="forces", matrix=False, **_):
+        """
+        Nuclear Hessian (nat, 3, nat, 3), or (3 nat, 3 nat) with ``matrix``
+        (calculators/types/autograd.py:198-329). All 6 nat displaced single
+        points run as one packed batch with analytic gradients
+        (``dxtb_gb300.hessian``); ``use_functorch`` and ``derived_quantity``
+        select autodiff variants in the reference and are accepted here. The
+        displaced SCFs are converged in implicit mode to min(x_atol, 1e-10).
+        """
+        if self.batched:
+            raise NotImplementedError(
+                "Hessian calculation is not supported in batch mode. "
+                "Please use the single system mode."
+            )
+        if derived_quantity not in ("energy", "forces"):
+            raise ValueError(f"Unknown derived quantity '{derived_quantity}'.")
+        self._check(positions)
+        from .hessian import hessian
+
+        spins = None if spin is None else int(spin)
+        return hessian(self.tables, self._mols[0], positions.detach(), chrg=float(chrg), spin=spins,
+                       etemp=self.etemp, tol=min(self.tol, 1e-10), maxiter=max(self.maxiter, 250),
+                       matrix=matrix, device=self.device)
 
     def singlepoint(self, positions, chrg=0, spin=None) -> Result:
         """The single point as a ``Result`` (calculators/types/energy.py:78-414)."""

@@ -10,7 +10,10 @@ integral wrappers and PyTorch driver classes.
   dipole,quadrupole}.py``.
 
 All three come from one launch of the McMurchie-Davidson kernel
-(``dxtb_multipole_raw``, one warp per shell pair). The dipole is (3, nao,
+(``dxtb_multipole_raw``, one warp per shell pair). With
+``positions.requires_grad`` the wrappers return tensors whose backward is
+the integral VJP kernel (``dxtb_multipole_raw_vjp``), as the reference's
+wrappers carry autograd. The dipole is (3, nao,
 nao) and the quadrupole (9, nao, nao) in the order xx xy xz yx yy yz zx zy
 zz. The moment operators are taken about the origin, as the reference
 wrappers return them. A batch (2D zero-padded ``numbers``) gives
@@ -149,10 +152,47 @@ IntDriverPytorch = IntDriver
 OverlapPytorch, DipolePytorch, QuadrupolePytorch = Overlap, Dipole, Quadrupole
 
 
+class _RawIntegral(torch.autograd.Function):
+    """Integral matrices with the VJP kernel as backward."""
+
+    @staticmethod
+    def forward(ctx, positions, drv, kind):
+        drv.setup(positions.detach())
+        ctx.drv, ctx.kind, ctx.shape = drv, kind, positions.shape
+        return drv.matrices(kind).clone()
+
+    @staticmethod
+    def backward(ctx, gout):
+        drv, kind = ctx.drv, ctx.kind
+        pb = drv._pb
+        ncomp = {"S": 1, "D": 3, "Q": 9}[kind]
+        mtot = pb.total["mat"]
+        flat = torch.zeros(ncomp, max(mtot, 1), dtype=torch.float64, device=drv.device)
+        g = gout.reshape(pb.nmol if drv.batched else 1, ncomp, gout.shape[-2], gout.shape[-1]) \
+            if ncomp > 1 else gout.reshape(-1, 1, gout.shape[-2], gout.shape[-1])
+        for i in range(pb.nmol):
+            n, m0 = int(pb.nao[i]), int(pb.mat_off[i])
+            flat[:, m0 : m0 + n * n] = g[i, :, :n, :n].reshape(ncomp, n * n)
+        grad = torch.zeros(pb.total["atoms"], 3, dtype=torch.float64, device=drv.device)
+        ptrs = {"S": None, "D": None, "Q": None}
+        ptrs[kind] = flat.data_ptr()
+        L = _lib.lib()
+        _lib.check(L.dxtb_multipole_raw_vjp(C.byref(pb.struct), pb.t["par_f"].data_ptr(),
+                                            pb.t["par_i"].data_ptr(), ptrs["S"], ptrs["D"], ptrs["Q"],
+                                            grad.data_ptr(), _lib.stream_ptr()), "integral VJP")
+        out = torch.zeros(ctx.shape, dtype=torch.float64, device=drv.device).reshape(-1, ctx.shape[-2], 3)
+        for i in range(pb.nmol):
+            a0, a1 = int(pb.atom_off[i]), int(pb.atom_off[i + 1])
+            out[i, : a1 - a0] = grad[a0:a1]
+        return out.reshape(ctx.shape), None, None
+
+
 def _integral(kind: str, numbers, positions, par, **kwargs) -> torch.Tensor:
     kwargs.pop("normalize", None)
     kwargs.pop("driver", None)
     drv = IntDriver(numbers, par, device=positions.device if positions.is_cuda else None)
+    if positions.requires_grad:
+        return _RawIntegral.apply(positions, drv, kind)
     drv.setup(positions)
     return drv.matrices(kind)
 

@@ -222,6 +222,18 @@ typedef struct dxtb_scf_config {
   double diagonal_offset;
 } dxtb_scf_config;
 
+/* Backward of dxtb_multipole_raw: accumulates into grad [natoms][3] the
+ * vector-Jacobian product dL/dR = sum dL/dM_k dM_k/dR of the normalised
+ * integrals about the origin for the upstream gradients grad_overlap [mat],
+ * grad_dipole [3][mat] and grad_quadrupole [9][mat] (row-major xx..zz; any
+ * may be null). The reference obtains it by autograd through the integral
+ * wrappers (integral/wrappers.py:149-215). */
+int32_t dxtb_multipole_raw_vjp(const dxtb_batch *b, const double *par_f,
+                               const int32_t *par_i, const double *grad_overlap,
+                               const double *grad_dipole,
+                               const double *grad_quadrupole, double *grad,
+                               void *stream);
+
 /* SCF workspace of one molecule in doubles (n AOs, nat atoms); the caller
  * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
 int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);

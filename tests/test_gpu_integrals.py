@@ -65,3 +65,29 @@ def test_driver_classes_batched_padding():
         assert np.abs(D[i, :, :k, :k].cpu().numpy() - d).max() < 1e-12
         assert np.abs(Q[i, :, :k, :k].cpu().numpy() - q).max() < 1e-11
         assert float(S[i, k:].abs().sum()) == 0.0 and float(S[i, :, k:].abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+@pytest.mark.parametrize("name", ["H2O", "SiH4"])
+def test_wrapper_gradients_match_oracle_autograd(method, name):
+    """The wrappers' backward (the VJP kernel) against autograd through the
+    oracle's integrals, for random upstream gradients of S, D and Q."""
+    from dxtb_gb300.integrals import dipint, overlap, quadint
+
+    num = torch.tensor(G[f"{name}/numbers"])
+    p0 = torch.tensor(G[f"{name}/positions"])
+    sysm = X.make_system(method, num.numpy())
+    gen = torch.Generator().manual_seed(7)
+    for fn, comps, kind in ((overlap, X.COMP_S, 0), (dipint, X.COMP_D, 1), (quadint, X.COMP_Q9, 2)):
+        pos = p0.clone().cuda().requires_grad_(True)
+        m = fn(num, pos, method)
+        up = torch.randn(m.shape, generator=gen, dtype=torch.float64)
+        (g_gpu,) = torch.autograd.grad((m * up.cuda()).sum(), pos)
+        pc = p0.clone().requires_grad_(True)
+        raw = X.multipole_raw(sysm, pc, comps)
+        norm = X.snorm(X.multipole_raw(sysm, pc, X.COMP_S)[0])
+        ref = raw * (norm[:, None] * norm[None, :])
+        if kind == 0:
+            ref = ref[0]
+        (g_ref,) = torch.autograd.grad((ref * up).sum(), pc)
+        assert np.abs(g_gpu.cpu().numpy() - g_ref.numpy()).max() < 1e-10, fn.__name__

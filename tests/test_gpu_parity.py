@@ -217,3 +217,59 @@ def test_reference_default_options(method):
     assert int(res.iter[0]) == ref.iterations + 2  # guess-mixing pass and the final evaluation
     assert abs(e - ref.energy) < E_TOL
     assert np.abs(f + ref.extra["gradient"].numpy()).max() < F_TOL
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_hessian_vs_oracle_finite_differences(method):
+    """The batched Hessian (6 nat displaced single points in one packed batch)
+    against central differences of the oracle's gradient (h = 1e-4 Bohr,
+    SCF to 1e-12), and its symmetry and translational invariance."""
+    from dxtb_gb300.workloads import random_molecule
+
+    num, pos = random_molecule(2200 + (method == "gfn2"), 7)
+    c = calc(method, num)
+    hs = c.hessian(torch.tensor(pos, device="cuda"), matrix=True).cpu().numpy()
+    nat = len(num)
+    assert hs.shape == (3 * nat, 3 * nat)
+    h = 1e-4
+    ref = np.zeros((3 * nat, 3 * nat))
+    for a in range(nat):
+        for x in range(3):
+            g = []
+            for sgn in (1.0, -1.0):
+                q = pos.copy()
+                q[a, x] += sgn * h
+                g.append(X.singlepoint(method, num, q, grad=True, tol=1e-12).extra["gradient"].numpy())
+            ref[3 * a + x] = ((g[0] - g[1]) / (2 * h)).ravel()
+    ref = 0.5 * (ref + ref.T)
+    assert np.abs(hs - ref).max() < 2e-5
+    # a rigid translation costs nothing: rows sum to zero over each axis
+    assert np.abs(hs.reshape(3 * nat, nat, 3).sum(1)).max() < 2e-5
+
+
+def test_autotune_applies_and_caches(tmp_path, monkeypatch):
+    """The size-class autotuner times its candidates, applies the fastest,
+    caches it per GPU and batch shape, and leaves results unchanged."""
+    import json
+
+    from dxtb_gb300 import autotune
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.workloads import config_molecules
+
+    monkeypatch.setenv("DXTB_CACHE_DIR", str(tmp_path))
+    before = autotune.get_classes()
+    mols = config_molecules(2, count=40)
+    pb = PackedBatch(tables("gfn2"), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols])
+    e0 = run(pb).energy.cpu().numpy()
+    try:
+        cands = [autotune.DEFAULT, (100, 136, 160, 320, 640)]
+        out = autotune.tune(pb, candidates=cands, reps=1)
+        assert tuple(out["thresholds"]) in cands
+        assert autotune.get_classes() == tuple(out["thresholds"])
+        data = json.loads((tmp_path / "autotune.json").read_text())
+        assert any(out["thresholds"] == v["thresholds"] for d in data.values() for v in d.values())
+        e1 = run(pb).energy.cpu().numpy()
+        assert np.abs(e1 - e0).max() < 1e-10
+    finally:
+        autotune.set_classes(before)
