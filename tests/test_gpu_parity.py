@@ -201,7 +201,9 @@ def test_reference_default_options(method):
     from dxtb_gb300 import GFN1Calculator, GFN2Calculator
     from dxtb_gb300.workloads import random_molecule
 
-    num, pos = random_molecule(2100 + (method == "gfn2"), 24)
+    # (seed 2100 is an SCF with several solutions: the reference loop itself
+    # does not converge there within 100 iterations)
+    num, pos = random_molecule(2104 if method == "gfn1" else 2101, 24)
     cls = GFN1Calculator if method == "gfn1" else GFN2Calculator
     with warnings.catch_warnings(record=True) as w:
         warnings.simplefilter("always")
