@@ -235,10 +235,14 @@ def cpu_reference(mols, sample: int, method="gfn2"):
 E2E_OPTS = {"exclude": ["disp", "d4sc"], "scf_mode": "implicit", "x_atol": 1e-10, "f_atol": 1e-10,
             "maxiter": 250, "guess": "sad"}
 
-# DRAM bytes (read + write) of the SCF launches per step, from the ncu
-# capture of the SCF kernels summarised under profiles/ (None until measured)
-SCF_TRAFFIC = None
-SCF_TRAFFIC_SOURCE = None
+# DRAM bytes (read + write) of the SCF launches per step: the ncu capture of
+# every SCF size class on the first 16 molecules (19.33 MB for a sum of n^2 of
+# 138,431, profiles/k_scf_classes_and_grad_pairs_16mol.md) scaled to the 256
+# molecules by the sum of n^2 (2,392,388); the SCF's DRAM traffic is its
+# O(n^2) inputs and outputs, its O(n^3) work stays in L2 and shared memory
+SCF_TRAFFIC = 19.33e6 / 138431 * 2392388
+SCF_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the four SCF launches, "
+                      "16 molecules, scaled by sum n^2 to the 256-molecule step")
 
 
 def measured_hbm_gbs() -> float | None:

@@ -1,0 +1,43 @@
+"""
+Oracle fixture of one large molecule for the GPU parity test above n = 1000:
+GFN2 + generalized Born (Still kernel, epsilon = 78.4, the solvation of the
+large-system configuration) on the seeded random-walk molecule of 401 atoms
+(seed 5100), energy and gradient, SCF to 1e-10.
+
+    python tests/golden/make_large_fixture.py
+
+Writes ``large_gb.npz`` (numbers, positions, energy, gradient, iterations).
+"""
+
+from __future__ import annotations
+
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+SEED, NAT = 5100, 400
+SOLVATION = {"epsilon": 78.4, "alpb": False, "kernel": "still"}
+
+
+def main() -> None:
+    from dxtb_gb300.workloads import random_molecule
+    from oracle import xtb_oracle as X
+
+    z, p = random_molecule(SEED, NAT)
+    t = time.time()
+    r = X.singlepoint("gfn2", z, p, tol=1e-10, maxiter=250, solvation=SOLVATION, grad=True)
+    np.savez_compressed(
+        HERE / "large_gb.npz", numbers=z, positions=p, energy=np.array(r.energy),
+        gradient=r.extra["gradient"].numpy(), iterations=np.array(r.iterations),
+        converged=np.array(r.extra["converged"]), seed=np.array(SEED), nat_request=np.array(NAT),
+    )
+    print(f"{len(z)} atoms, {r.iterations} iterations, E = {r.energy:.10f} ({time.time() - t:.0f} s)")
+
+
+if __name__ == "__main__":
+    main()

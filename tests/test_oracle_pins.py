@@ -176,3 +176,22 @@ def test_gfn1_alpb_solvation_energy_and_gradient():
     assert abs((sol.e_elec - vac.e_elec) - gsolv) < 1e-7
     # the fixture differentiates E_scf (no -TS); the reference's tolerance is 1e-5
     assert np.abs(sol.extra["gradient"].numpy() - G["solv/MB16_43_01/gradient"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_anderson_loop_reaches_the_pinned_solution(method):
+    """The restated full-mode loop (Anderson mixer) converges to the fixed
+    point of the implicit-mode root solver, whose energies the fixtures
+    above pin: to 1e-10 Eh with tight tolerances, and to the tolerance's
+    order with the reference defaults (x_atol 1e-4, x_atol_max 1e-5)."""
+    from dxtb_gb300.workloads import random_molecule
+
+    num, pos = random_molecule(2104 if method == "gfn1" else 2101, 12)
+    ref = X.singlepoint(method, num, pos, tol=1e-12)
+    tight = X.singlepoint(method, num, pos, mixer="anderson", maxiter=200,
+                          anderson={"x_atol": 1e-11, "x_atol_max": 1e-12})
+    loose = X.singlepoint(method, num, pos, mixer="anderson", maxiter=100)
+    assert tight.extra["converged"] and loose.extra["converged"]
+    assert abs(tight.energy - ref.energy) < 1e-10
+    assert abs(loose.energy - ref.energy) < 1e-6
+    assert loose.iterations < tight.iterations
