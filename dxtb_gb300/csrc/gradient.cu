@@ -100,6 +100,10 @@ struct GPair {
   double A[3], B[3];
 };
 
+// Shell pairs without a p-p or d product take one thread each
+// (k_grad_pairs_sp); the warp kernel leaves them out.
+__device__ __forceinline__ bool gsp_class(int la, int lb) { return la + lb <= 1; }
+
 // One shell pair of the integral adjoint (one warp).
 __device__ __forceinline__ void grad_pair(
     const dxtb_batch &b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
@@ -107,13 +111,13 @@ __device__ __forceinline__ void grad_pair(
     const double *__restrict__ S, const double *__restrict__ D, const double *__restrict__ vorb,
     const double *__restrict__ vdp, const double *__restrict__ vqp, int multipole,
     double *__restrict__ dedcn, double *__restrict__ grad, int64_t k, int lane, double *s_tab,
-    double *s_esph, double *s_ecart) {
+    double *s_esph, double *s_ecart, bool skip_sp) {
 
   GPair g;
   g.m = find_mol(b.pair_off, b.nmol, k);
   {
     const int64_t t = k - b.pair_off[g.m];
-    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    int i = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
     while ((int64_t)(i + 1) * (i + 2) / 2 <= t) ++i;
     while ((int64_t)i * (i + 1) / 2 > t) --i;
     g.i = i;
@@ -133,6 +137,7 @@ __device__ __forceinline__ void grad_pair(
   }
   g.la = pi_(pi_tab, DXTB_I_L + g.ti);
   g.lb = pi_(pi_tab, DXTB_I_L + g.tj);
+  if (skip_sp && gsp_class(g.la, g.lb)) return;  // uniform over the warp
   g.na = pi_(pi_tab, DXTB_I_NPRIM + g.ti);
   g.nb = pi_(pi_tab, DXTB_I_NPRIM + g.tj);
   const int la = g.la, lb = g.lb, nsa = 2 * la + 1, nsb = 2 * lb + 1;
@@ -340,8 +345,249 @@ __global__ void __launch_bounds__(gWarps * 32)
   for (int64_t k = (int64_t)blockIdx.x * gWarps + w; k < npairs; k += (int64_t)gridDim.x * gWarps) {
     if (flt.cls >= 0 && !in_class(flt, b, find_mol(b.pair_off, b.nmol, k))) continue;  // warp-uniform
     grad_pair(b, pf_, pi_tab, cn, P, W, S, D, vorb, vdp, vqp, multipole, dedcn, grad, k, lane, s_tab,
-              s_esph, s_ecart);
+              s_esph, s_ecart, true);
     __syncwarp();  // the next pair reuses this warp's shared tables
+  }
+}
+
+// One s-s or s-p shell pair of the integral adjoint on one thread: the
+// coefficient blocks and the bra-derivative contraction of grad_pair, with
+// the s shell on the bra (a p-s pair is evaluated as its s-p mirror, which
+// holds the same two matrix elements; the pair's contribution is symmetric
+// under exchanging bra and ket), the tables written out for l <= 1 and the
+// spherical transform the identity.
+template <int LB, int NC>
+__device__ __forceinline__ void grad_pair_sp(
+    const dxtb_batch &b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
+    const double *__restrict__ cn, const double *__restrict__ P, const double *__restrict__ W,
+    const double *__restrict__ S, const double *__restrict__ D, const double *__restrict__ vorb,
+    const double *__restrict__ vdp, const double *__restrict__ vqp, double *__restrict__ dedcn,
+    double *__restrict__ grad, const GPair &g) {
+  constexpr int NSB = 2 * LB + 1;
+  constexpr bool MP = NC > 1;
+  const int64_t moff = b.mat_off[g.m], mtot = b.mat_off[b.nmol];
+  const int n = (int)(b.ao_off[g.m + 1] - b.ao_off[g.m]);
+  const int64_t o0 = b.ao_off[g.m];
+  const int oi = b.shell_ao[g.gi], oj = b.shell_ao[g.gj];
+  const bool same_atom = (g.ai == g.aj);
+  const int zi = b.numbers[g.a0 + g.ai], zj = b.numbers[g.a0 + g.aj];
+  const double sei = pf(pf_, DXTB_P_LEVEL + g.ti) - pf(pf_, DXTB_P_KCN + g.ti) * cn[g.a0 + g.ai];
+  const double sej = pf(pf_, DXTB_P_LEVEL + g.tj) - pf(pf_, DXTB_P_KCN + g.tj) * cn[g.a0 + g.aj];
+  double fk = 1.0, pi = 1.0, dpi = 0.0, dist = 0.0;
+  const double d[3] = {g.B[0] - g.A[0], g.B[1] - g.A[1], g.B[2] - g.A[2]};
+  if (!same_atom) {
+    dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double rsum = pf(pf_, DXTB_P_RAD + zi) + pf(pf_, DXTB_P_RAD + zj);
+    const double rr = sqrt(dist / rsum);
+    const double ki = pf(pf_, DXTB_P_SHPOLY + g.ti), kj = pf(pf_, DXTB_P_SHPOLY + g.tj);
+    pi = (1.0 + ki * rr) * (1.0 + kj * rr);
+    dpi = (ki * (1.0 + kj * rr) + kj * (1.0 + ki * rr)) * rr / (2.0 * dist);
+    const int vi = pi_(pi_tab, DXTB_I_VALENCE + g.ti), vj = pi_(pi_tab, DXTB_I_VALENCE + g.tj);
+    const double wexp = pf(pf_, DXTB_P_SCAL + DXTB_S_WEXP);
+    const double zti = pf(pf_, DXTB_P_SLATER + g.ti), ztj = pf(pf_, DXTB_P_SLATER + g.tj);
+    const double zfac = wexp == 0.0 ? 1.0 : pow(2.0 * sqrt(zti * ztj) / (zti + ztj), wexp);
+    if (vi && vj) {
+      const double den = pf(pf_, DXTB_P_EN + zi) - pf(pf_, DXTB_P_EN + zj);
+      fk = pf(pf_, DXTB_P_KSHELL + g.la * 5 + g.lb) * zfac * pf(pf_, DXTB_P_KPAIR + zi * DXTB_MAXZ + zj) *
+           (1.0 + pf(pf_, DXTB_P_SCAL + DXTB_S_ENSCALE) * den * den);
+    } else {
+      const double kpol = pf(pf_, DXTB_P_SCAL + DXTB_S_KPOL);
+      const double kii = vi ? pf(pf_, DXTB_P_KSHELL + g.la * 6) : kpol;
+      const double kjj = vj ? pf(pf_, DXTB_P_KSHELL + g.lb * 6) : kpol;
+      fk = 0.5 * (kii + kjj) * zfac;
+    }
+  }
+  const double h = 0.5 * (sei + sej) * pi * fk;
+  const int64_t A0 = g.a0 + g.ai, B0 = g.a0 + g.aj;
+  double ps = 0.0, gconst[3] = {0.0, 0.0, 0.0};
+  double es[NSB][NC];
+#pragma unroll
+  for (int mb = 0; mb < NSB; ++mb) {
+    const int mu = oi, nu = oj + mb;
+    const int64_t e1 = moff + (int64_t)mu * n + nu;
+    const double Pmn = P[e1], Smn = S[e1];
+    ps += Pmn * Smn;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) es[mb][c] = 0.0;
+    if (same_atom) continue;
+    const double cS2 = 2.0 * (Pmn * h - 0.5 * Pmn * (vorb[o0 + mu] + vorb[o0 + nu]) - W[e1]);
+    if constexpr (!MP) {
+      es[mb][0] = cS2;
+    } else {
+      const int qa[6] = {0, 0, 1, 0, 1, 2}, qb[6] = {0, 1, 1, 2, 2, 2};
+      const int q2comp[6] = {4, 5, 7, 6, 8, 9};
+      double cDA[3], cDB[3], cQA[6], cQB[6], tA[6], tB[6];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        cDB[x] = -Pmn * vdp[3 * B0 + x];
+        cDA[x] = -Pmn * vdp[3 * A0 + x];
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        tB[c] = -Pmn * vqp[6 * B0 + c];
+        tA[c] = -Pmn * vqp[6 * A0 + c];
+      }
+      const double trA = 0.5 * (tA[0] + tA[2] + tA[5]), trB = 0.5 * (tB[0] + tB[2] + tB[5]);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const bool diag = (c == 0 || c == 2 || c == 5);
+        cQA[c] = 1.5 * tA[c] - (diag ? trA : 0.0);
+        cQB[c] = 1.5 * tB[c] - (diag ? trB : 0.0);
+      }
+      double eS = cS2, eD[3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        eS += cDA[x] * d[x];
+        eD[x] = cDB[x] + cDA[x];
+      }
+      double DB[3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) DB[x] = D[x * mtot + e1];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const int a = qa[c], bq = qb[c];
+        eS += cQA[c] * d[a] * d[bq];
+        eD[a] += cQA[c] * d[bq];
+        eD[bq] += cQA[c] * d[a];
+        es[mb][q2comp[c]] = cQB[c] + cQA[c];
+        gconst[bq] -= cQA[c] * (DB[a] + d[a] * Smn);
+        gconst[a] -= cQA[c] * (DB[bq] + d[bq] * Smn);
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) gconst[x] -= cDA[x] * Smn;
+      es[mb][0] = eS;
+#pragma unroll
+      for (int x = 0; x < 3; ++x) es[mb][1 + x] = eD[x];
+    }
+  }
+  {
+    const double f = same_atom ? 1.0 : pi * fk;
+    atomicAdd(&dedcn[A0], -pf(pf_, DXTB_P_KCN + g.ti) * f * ps);
+    if (g.i != g.j) atomicAdd(&dedcn[B0], -pf(pf_, DXTB_P_KCN + g.tj) * f * ps);
+  }
+  if (same_atom) return;
+  // contraction with d/dA of the Cartesian integrals (moments about B)
+  double gx = 0.0, gy = 0.0, gz = 0.0;
+  const double r2 = dist * dist;
+  for (int p1 = 0; p1 < g.na; ++p1) {
+    const double a = pf(pf_, DXTB_P_ALPHA + g.ti * DXTB_MAXPRIM + p1);
+    const double ca = pf(pf_, DXTB_P_COEFF + g.ti * DXTB_MAXPRIM + p1);
+    for (int p2 = 0; p2 < g.nb; ++p2) {
+      const double bb = pf(pf_, DXTB_P_ALPHA + g.tj * DXTB_MAXPRIM + p2);
+      const double cb = pf(pf_, DXTB_P_COEFF + g.tj * DXTB_MAXPRIM + p2);
+      const double oij = 1.0 / (a + bb), x2p = 0.5 * oij;
+      const double sij = exp(-a * bb * oij * r2) * (kPi * sqrt(kPi)) * oij * sqrt(oij) * ca * cb;
+      // T[x][c][e] (bra power 0) and dT[x][c][e] = 2 alpha T(bra power 1):
+      // E[0][0] = {1}, E[1][0] = {xpa, x2p}, E[0][1] = {xpb, x2p},
+      // E[1][1] = {xpb xpa + x2p, xpb x2p + x2p xpa, x2p^2}, moments about B
+      double T[3][2][3], dT[3][2][3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        const double Pc = (a * g.A[x] + bb * g.B[x]) * oij;
+        const double xpa = Pc - g.A[x], xpb = Pc - g.B[x];
+        const double m10 = xpb, m20 = xpb * xpb + x2p, m21 = 2.0 * xpb;
+        const double pref = x == 0 ? sij : 1.0;
+        T[x][0][0] = pref * 1.0;
+        T[x][0][1] = MP ? pref * (m10 * 1.0 + 0.0) : 0.0;
+        T[x][0][2] = MP ? pref * (m20 * 1.0 + m21 * 0.0 + 2.0 * 0.0) : 0.0;
+        dT[x][0][0] = pref * (2.0 * a * xpa);
+        dT[x][0][1] = MP ? pref * (2.0 * a * (m10 * xpa + x2p)) : 0.0;
+        dT[x][0][2] = MP ? pref * (2.0 * a * (m20 * xpa + m21 * x2p + 2.0 * 0.0)) : 0.0;
+        if (LB == 1) {
+          const double e0 = xpb * xpa + x2p, e1 = xpb * x2p + x2p * xpa, e2 = x2p * x2p;
+          T[x][1][0] = pref * xpb;
+          T[x][1][1] = MP ? pref * (m10 * xpb + x2p) : 0.0;
+          T[x][1][2] = MP ? pref * (m20 * xpb + m21 * x2p + 2.0 * 0.0) : 0.0;
+          dT[x][1][0] = pref * (2.0 * a * e0);
+          dT[x][1][1] = MP ? pref * (2.0 * a * (m10 * e0 + e1)) : 0.0;
+          dT[x][1][2] = MP ? pref * (2.0 * a * (m20 * e0 + m21 * e1 + 2.0 * e2)) : 0.0;
+        }
+      }
+#pragma unroll
+      for (int cb_ = 0; cb_ < NSB; ++cb_) {
+        // p order (y, z, x): component cb_ raises axis (cb_ + 1) % 3
+        const int px = LB == 1 && cb_ == 2, py = LB == 1 && cb_ == 0, pz = LB == 1 && cb_ == 1;
+#pragma unroll
+        for (int comp = 0; comp < NC; ++comp) {
+          const int ex = comp == 1 ? 1 : (comp == 4 ? 2 : (comp == 5 || comp == 6 ? 1 : 0));
+          const int ey = comp == 2 ? 1 : (comp == 7 ? 2 : (comp == 5 || comp == 8 ? 1 : 0));
+          const int ez = comp == 3 ? 1 : (comp == 9 ? 2 : (comp == 6 || comp == 8 ? 1 : 0));
+          const double coef = es[cb_][comp];
+          const double Tx = T[0][px][ex], Ty = T[1][py][ey], Tz = T[2][pz][ez];
+          gx = fma(coef, dT[0][px][ex] * Ty * Tz, gx);
+          gy = fma(coef, Tx * dT[1][py][ey] * Tz, gy);
+          gz = fma(coef, Tx * Ty * dT[2][pz][ez], gz);
+        }
+      }
+    }
+  }
+  gx += gconst[0];
+  gy += gconst[1];
+  gz += gconst[2];
+  const double dEdR = 2.0 * ps * h * dpi / pi;
+  const double u[3] = {-d[0] / dist, -d[1] / dist, -d[2] / dist};
+  const double gv[3] = {gx + dEdR * u[0], gy + dEdR * u[1], gz + dEdR * u[2]};
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    atomicAdd(&grad[3 * A0 + x], gv[x]);
+    atomicAdd(&grad[3 * B0 + x], -gv[x]);
+  }
+}
+
+template <int NC>
+__global__ void __launch_bounds__(128)
+    k_grad_pairs_sp(dxtb_batch b, const double *__restrict__ pf_, const int32_t *__restrict__ pi_tab,
+                    const double *__restrict__ cn, const double *__restrict__ P,
+                    const double *__restrict__ W, const double *__restrict__ S,
+                    const double *__restrict__ D, const double *__restrict__ vorb,
+                    const double *__restrict__ vdp, const double *__restrict__ vqp,
+                    double *__restrict__ dedcn, double *__restrict__ grad, ClassFilter flt) {
+  const int64_t npairs = b.pair_off[b.nmol];
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < npairs;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    GPair g;
+    g.m = find_mol(b.pair_off, b.nmol, k);
+    if (flt.cls >= 0 && !in_class(flt, b, g.m)) continue;
+    const int64_t t = k - b.pair_off[g.m];
+    int i = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while ((int64_t)(i + 1) * (i + 2) / 2 <= t) ++i;
+    while ((int64_t)i * (i + 1) / 2 > t) --i;
+    int j = (int)(t - (int64_t)i * (i + 1) / 2);
+    const int64_t s0 = b.shell_off[g.m];
+    g.a0 = b.atom_off[g.m];
+    int ti = b.shell_type[s0 + i], tj = b.shell_type[s0 + j];
+    int la = pi_(pi_tab, DXTB_I_L + ti), lb = pi_(pi_tab, DXTB_I_L + tj);
+    if (!gsp_class(la, lb)) continue;
+    if (la == 1) {  // evaluate the s-p mirror: the s shell on the bra
+      const int ii = i, tt = ti;
+      i = j;
+      j = ii;
+      ti = tj;
+      tj = tt;
+      la = 0;
+      lb = 1;
+    }
+    g.i = i;
+    g.j = j;
+    g.gi = s0 + i;
+    g.gj = s0 + j;
+    g.ti = ti;
+    g.tj = tj;
+    g.la = la;
+    g.lb = lb;
+    g.ai = b.shell_atom[g.gi];
+    g.aj = b.shell_atom[g.gj];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      g.A[x] = b.positions[3 * (g.a0 + g.ai) + x];
+      g.B[x] = b.positions[3 * (g.a0 + g.aj) + x];
+    }
+    g.na = pi_(pi_tab, DXTB_I_NPRIM + ti);
+    g.nb = pi_(pi_tab, DXTB_I_NPRIM + tj);
+    if (lb == 0)
+      grad_pair_sp<0, NC>(b, pf_, pi_tab, cn, P, W, S, D, vorb, vdp, vqp, dedcn, grad, g);
+    else
+      grad_pair_sp<1, NC>(b, pf_, pi_tab, cn, P, W, S, D, vorb, vdp, vqp, dedcn, grad, g);
   }
 }
 
@@ -567,6 +813,16 @@ int32_t launch_gradient(const dxtb_batch *b, const double *par_f, const int32_t 
     k_grad_pairs<<<(unsigned)blocks, gWarps * 32, gSmem, st>>>(*b, par_f, par_i, cn, density, wdensity,
                                                                overlap, dipole, vorb, vdp, vqp, multipole,
                                                                dedcn, grad, f);
+    DXTB_CHECK_LAUNCH();
+    // s-s and s-p pairs: a thread each
+    const int64_t tblocks = min((bound + 127) / 128, (int64_t)sms * 16);
+    if (multipole)
+      k_grad_pairs_sp<gNComp><<<(unsigned)tblocks, 128, 0, st>>>(*b, par_f, par_i, cn, density, wdensity,
+                                                                 overlap, dipole, vorb, vdp, vqp, dedcn,
+                                                                 grad, f);
+    else
+      k_grad_pairs_sp<1><<<(unsigned)tblocks, 128, 0, st>>>(*b, par_f, par_i, cn, density, wdensity, overlap,
+                                                            dipole, vorb, vdp, vqp, dedcn, grad, f);
     DXTB_CHECK_LAUNCH();
   }
   const size_t smem = sizeof(double) * (size_t)(b->max_nsh + 3 * b->max_nat + 8);

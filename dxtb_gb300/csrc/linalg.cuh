@@ -1016,9 +1016,11 @@ __device__ __forceinline__ void tri_vector_twisted(int n, const double *d, const
 // ~64 cycles whatever its active lanes, so this serial per-thread work is
 // written for few float64 instructions per row: pivots by integer compares,
 // no branches (selects), reciprocals of the pivots by rcp_nr (stored, so
-// the solves multiply), start vectors from integer bits, and no scaling
-// between the solves (the growth stays far inside the float64 range: at
-// most (n / tiny)^3); one normalisation at the end.
+// the solves multiply), start vectors from integer bits. Every solve starts
+// from a unit vector, and the back substitution rescales by 2^-600 when a
+// component passes 2^600: with several near-singular pivots (exactly
+// coincident eigenvalues of a split tridiagonal, common in large molecules
+// with distant, equivalent fragments) one solve can grow by (1 / tiny)^k.
 // d, e, lam: shared copies; e2s: shared scratch of n doubles (e^2). Y: n x m
 // row-major global (column j = vector j). lu: global scratch of
 // 5 * n * nslot doubles; team threads [0, nslot) factorise (nslot <= team
@@ -1084,8 +1086,26 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         LU(U0, n - 1) = rcp_nr(piv);
       }
       for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
+      // unit 2-norm of column j, scaled by its largest entry first so that
+      // the sum of squares cannot overflow
+      auto unit = [&]() {
+        double mx = 0.0;
+        for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Y[(size_t)i * m + j]));
+        const double s = mx > 0.0 ? 1.0 / mx : 1.0;
+        double nrm = 0.0;
+        for (int i = 0; i < n; ++i) {
+          const double v = Y[(size_t)i * m + j] * s;
+          nrm = fma(v, v, nrm);
+        }
+        const double inv = s / sqrt(fmax(nrm, kTiny));
+        for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+      };
       const int nsolve = (j1 - j0 > 1) ? 3 : 2;
       for (int it = 0; it < nsolve; ++it) {
+        // every solve starts from a unit vector: one solve grows it by up to
+        // ~1/tiny per near-singular pivot, and a cluster of exactly coincident
+        // eigenvalues (a split tridiagonal) has several of them
+        unit();
         // forward: apply the row interchanges and multipliers (the running
         // row stays in a register; the loads do not depend on the chain)
         double carry = Y[j];
@@ -1102,7 +1122,17 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         double x1 = 0.0, x2 = 0.0;
 #pragma unroll 4
         for (int i = n - 1; i >= 0; --i) {
-          const double v = fma(-LU(U2, i), x2, fma(-LU(U1, i), x1, Y[(size_t)i * m + j])) * LU(U0, i);
+          double v = fma(-LU(U2, i), x2, fma(-LU(U1, i), x1, Y[(size_t)i * m + j])) * LU(U0, i);
+          if (!(fabs(v) <= 0x1p600)) {
+            // growth beyond 2^600 (one row adds at most ~2^54: |U1|, |U2| <=
+            // 2 |T|, |U0| <= 1 / (eps |T|)): rescale the solved rows, the rest
+            // of the right-hand side and the carried values alike, and redo
+            // this row
+            for (int k = 0; k < n; ++k) Y[(size_t)k * m + j] *= 0x1p-600;
+            x1 *= 0x1p-600;
+            x2 *= 0x1p-600;
+            v = fma(-LU(U2, i), x2, fma(-LU(U1, i), x1, Y[(size_t)i * m + j])) * LU(U0, i);
+          }
           Y[(size_t)i * m + j] = v;
           x2 = x1;
           x1 = v;
@@ -1113,18 +1143,8 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
           for (int i = 0; i < n; ++i) dot = fma(Y[(size_t)i * m + k], Y[(size_t)i * m + j], dot);
           for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = fma(-dot, Y[(size_t)i * m + k], Y[(size_t)i * m + j]);
         }
-        if (j > j0 && it + 1 < nsolve) {
-          // keep the re-orthogonalised vector at unit scale for the next solve
-          double nrm = 0.0;
-          for (int i = 0; i < n; ++i) nrm = fma(Y[(size_t)i * m + j], Y[(size_t)i * m + j], nrm);
-          const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
-          for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
-        }
       }
-      double nrm = 0.0;
-      for (int i = 0; i < n; ++i) nrm = fma(Y[(size_t)i * m + j], Y[(size_t)i * m + j], nrm);
-      const double inv = 1.0 / sqrt(fmax(nrm, kTiny));
-      for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+      unit();
     }
   }
 #undef LU
