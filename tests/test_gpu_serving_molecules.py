@@ -1,0 +1,41 @@
+"""
+Regression: molecules of the seeded serving stream whose orbital spectra
+hold exactly coincident eigenvalue pairs during the SCF (a split tridiagonal:
+distant, equivalent fragments of a large random-walk molecule, n = 486-552).
+The inverse iteration of such a pair overflowed to NaN before its solves were
+rescaled. Energies and forces against the oracle fixtures of
+``golden/make_serving_fixture.py``, all four molecules in one packed batch
+per method (they run as 8-CTA clusters).
+"""
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-8   # Eh
+F_TOL = 1e-6   # Eh/Bohr
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_coincident_eigenvalue_molecules(method):
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+
+    d = np.load(Path(__file__).parent / "golden" / "serving_degenerate.npz")
+    rids = [int(r) for r in d["rids"] if str(d[f"{r}/method"]) == method and bool(d[f"{r}/converged"])]
+    assert rids
+    pb = PackedBatch(tables(method), [d[f"{r}/numbers"] for r in rids],
+                     [torch.tensor(d[f"{r}/positions"]) for r in rids])
+    res = run(pb, forces=True, tol=1e-10, maxiter=250)
+    st = res.status.cpu().numpy()
+    e = res.energy.cpu().numpy()
+    g = res.gradient.cpu().numpy()
+    for i, r in enumerate(rids):
+        assert st[i] == 0, (r, st[i])
+        assert abs(e[i] - float(d[f"{r}/energy"])) < E_TOL, r
+        gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
+        assert np.abs(gi - d[f"{r}/gradient"]).max() < F_TOL, r
