@@ -1,9 +1,8 @@
 """
 Oracle fixtures of four molecules of the seeded serving request stream
 (200 requests, Poisson, seed 4: requests 136 and 96 in GFN1, 48 in GFN1 and
-179 in GFN2, n = 486-552 orbitals) whose orbital spectra hold exactly
-coincident eigenvalue pairs during the SCF (distant, equivalent fragments
-of a random-walk molecule), energy and gradient, SCF to 1e-10.
+179 in GFN2, n = 486-552 orbitals) whose SCF passes through tight
+two-member eigenvalue clusters, energy and gradient, SCF to 1e-10.
 
     python tests/golden/make_serving_fixture.py
 

@@ -1,11 +1,11 @@
 """
-Regression: molecules of the seeded serving stream whose orbital spectra
-hold exactly coincident eigenvalue pairs during the SCF (a split tridiagonal:
-distant, equivalent fragments of a large random-walk molecule, n = 486-552).
-The inverse iteration of such a pair turned NaN before the factorisation
-zeroed its last row's super-diagonal slots. Energies and forces against the oracle fixtures of
-``golden/make_serving_fixture.py``, all four molecules in one packed batch
-per method (they run as 8-CTA clusters).
+Regression: molecules of the seeded serving stream (n = 486-552, 8-CTA
+clusters) whose SCF passes through tight two-member eigenvalue clusters,
+solved by inverse iteration. Their vectors turned NaN while the
+factorisation left its last row's super-diagonal slots unwritten (slots the
+twisted vectors fill with integer scale counts). Energies and forces of the
+well-conditioned ones against the oracle fixtures of
+``golden/make_serving_fixture.py``, in one packed batch per method.
 """
 
 from pathlib import Path
