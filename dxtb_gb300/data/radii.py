@@ -20,7 +20,7 @@ values below are the published tables those names refer to:
     MB16_43_01 and SiH4 in dxtb's ``test/test_solvation/samples.py``. A
     least-squares fit of all eight MB16_43_01 radii to its 16 psi values
     returns them at the 5-digit table values, with a relative residual of
-    2e-15 (``tests/golden/fit_vdw_radii.py``). C and S are the published
+    2e-15 (``tests/test_vdw_radii_fit.py``). C and S are the published
     table values; no fixture contains them.
 
 Only elements whose values are either pinned by the dxtb test fixtures
