@@ -33,6 +33,8 @@ EXCLUDE: dict = {
     ("c2", "gfn2"): {},
     ("c3", "gfn1"): {
         1: "oracle 116 iterations; the GPU trajectory does not settle within 250",
+        6: "oracle 105 iterations; the GPU reaches the oracle's energy (2.8e-14) and "
+           "forces (1.2e-10) but does not meet the 1e-10 stopping rule within 250",
         23: "oracle 137 iterations; the GPU lands on another SCF solution (0.22 Eh)",
         37: "oracle 145 iterations; the GPU trajectory does not settle within 250",
         48: "the oracle itself does not converge within 250 iterations",
