@@ -871,11 +871,15 @@ __device__ __forceinline__ bool abs_ge(double a, double b) {
 // eleven float64 instructions per row in all, against ~20 and four
 // memory-bound sweeps of the pivoted LU with two solves. P, Q, SP, SQ: per-thread scratch columns of n doubles (stride
 // nslot, column tid). Writes the normalised vector to column j of Y (n x m).
-__device__ __forceinline__ void tri_vector_twisted(int n, const double *d, const double *e,
-                                                   const double *e2, double lmb, double *__restrict__ Y,
-                                                   int m, int j, double *__restrict__ P,
-                                                   double *__restrict__ Q, double *__restrict__ SP,
-                                                   double *__restrict__ SQ, int nslot, int tid) {
+// Returns the Rayleigh-quotient correction gamma_r / |z|^2 of lmb: with
+// z_r = 1 the twisted vector satisfies (T - lmb I) z = gamma_r e_r, so a
+// correction above the rounding level means lmb was not accurate enough for
+// this vector (its error is about |correction| / gap).
+__device__ __forceinline__ double tri_vector_twisted(int n, const double *d, const double *e,
+                                                     const double *e2, double lmb, double *__restrict__ Y,
+                                                     int m, int j, double *__restrict__ P,
+                                                     double *__restrict__ Q, double *__restrict__ SP,
+                                                     double *__restrict__ SQ, int nslot, int tid) {
 #define AT(arr, i) arr[(size_t)(i) * nslot + tid]
   auto expo = [](double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7ff); };
   auto keep = [&](double &a, double &b, int &cnt) {
@@ -1000,9 +1004,14 @@ __device__ __forceinline__ void tri_vector_twisted(int n, const double *d, const
       keep(E, one, cnt);
     }
   }
+  // residual of the twist row: gamma_r = e_{r-1} z_{r-1} + (d_r - lmb) + e_r z_{r+1}
+  double gam = d[r] - lmb;
+  if (r > 0) gam = fma(e[r - 1], Y[(size_t)(r - 1) * m + j], gam);
+  if (r + 1 < n) gam = fma(e[r], Y[(size_t)(r + 1) * m + j], gam);
   const double inv = 1.0 / sqrt(nrm);
 #pragma unroll 4
   for (int i = 0; i < n; ++i) Y[(size_t)i * m + j] *= inv;
+  return gam / nrm;
 #undef AT
 }
 
@@ -1054,7 +1063,16 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
   for (int c = tid; tid < nslot && c < ncl; c += nslot) {
     const int j0 = ldi<CL>(cl + c), j1 = ldi<CL>(cl + c + 1);
     if (j1 - j0 == 1 && twist_ok) {
-      tri_vector_twisted(n, d, e, e2s, lam[j0], Y, m, j0, U0, U1, U2, Lm, nslot, tid);
+      // one Rayleigh-quotient step when the eigenvalue is off by more than
+      // rounding (Newton's root of a long recurrence can be ~1e-10 |T| off,
+      // which spoils the vector of an eigenvalue with a gap of ~1e-6 |T|);
+      // the refined shift is accurate to ~delta^2 / gap
+      double lmb = lam[j0];
+      for (int pass = 0; pass < 2; ++pass) {
+        const double delta = tri_vector_twisted(n, d, e, e2s, lmb, Y, m, j0, U0, U1, U2, Lm, nslot, tid);
+        if (!(fabs(delta) > 8.0 * kEps * fmax(tnorm, 1.0))) break;
+        lmb += delta;
+      }
       continue;
     }
     for (int j = j0; j < j1; ++j) {
