@@ -1043,7 +1043,13 @@ __device__ void team_tri_vectors(Team<CL> &tm, int n, const double *d, const dou
   for (int i = threadIdx.x; i < n; i += blockDim.x) e2s[i] = i < n - 1 ? e[i] * e[i] : 0.0;
   // the twisted vector's range bookkeeping (rescaling every fourth row)
   // assumes |T| within 2^-+16 (a Fock matrix in Hartree: ~1..100)
-  const bool twist_ok = tnorm < 0x1p16 && tnorm > 0x1p-16;
+  // Above 384 orbitals every vector takes inverse iteration: there the
+  // twisted vectors of some molecules stalled the SCF near a residual of
+  // 1e-2 (n = 743 and 796 in the serving stream, with or without the
+  // Rayleigh-quotient step below), where inverse iteration follows the
+  // oracle's trajectory exactly; every molecule of the benchmark sets (n <=
+  // 377) is verified against the oracle with the twisted path.
+  const bool twist_ok = n <= 384 && tnorm < 0x1p16 && tnorm > 0x1p-16;
   if (tm.lead() && threadIdx.x == 0) {
     int c = 0;
     cl[c++] = 0;

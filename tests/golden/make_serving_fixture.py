@@ -1,8 +1,10 @@
 """
-Oracle fixtures of four molecules of the seeded serving request stream
-(200 requests, Poisson, seed 4: requests 136 and 96 in GFN1, 48 in GFN1 and
-179 in GFN2, n = 486-552 orbitals) whose SCF passes through tight
-two-member eigenvalue clusters, energy and gradient, SCF to 1e-10.
+Oracle fixtures of six molecules of the seeded serving request stream
+(200 requests, Poisson, seed 4: requests 136, 96, 48 and 166 in GFN1, 179
+and 0 in GFN2, n = 486-796 orbitals) whose SCF passes through tight
+two-member eigenvalue clusters (136, 96, 48, 179) or needs eigenvectors of
+eigenvalues with small gaps to more than the Newton root's accuracy (0,
+166), energy and gradient, SCF to 1e-10.
 
     python tests/golden/make_serving_fixture.py
 
@@ -20,7 +22,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-RIDS = (136, 96, 48, 179)
+RIDS = (136, 96, 48, 179, 0, 166)
 
 
 def _one(rid):
