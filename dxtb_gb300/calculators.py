@@ -378,6 +378,67 @@ class Calculator:
                        etemp=self.etemp, tol=min(self.tol, 1e-10), maxiter=max(self.maxiter, 250),
                        matrix=matrix, device=self.device)
 
+    # ---- properties (calculators/types/autograd.py:331-995) ----
+    def dipole(self, positions, chrg=0, spin=None, **_):
+        """
+        Electric dipole moment (3,) (or (B, 3) batched) in e a0 at the
+        converged density: sum_A Z_A R_A - tr(P D0)
+        (``calculators/properties/moments/dip.py``), one ``dxtb_dipole_moment``
+        launch for the batch. The reference also obtains it as -dE/dF through
+        its electric-field interaction; at zero field the two agree (its
+        ``test_properties/test_dipole.py`` asserts it).
+        """
+        from .properties import dipole_moments
+
+        r = self._run(positions.detach(), chrg, spin)
+        mu = dipole_moments(self._pb, r["result"].state["P"])
+        return mu if self.batched else mu[0]
+
+    dipole_analytical = dipole
+
+    def _hessian_dipole(self, positions, chrg, spin):
+        if self.batched:
+            raise NotImplementedError(
+                "Hessian calculation is not supported in batch mode. "
+                "Please use the single system mode."
+            )
+        self._check(positions)
+        from .hessian import hessian
+
+        spins = None if spin is None else int(spin)
+        return hessian(self.tables, self._mols[0], positions.detach(), chrg=float(chrg), spin=spins,
+                       etemp=self.etemp, tol=min(self.tol, 1e-10), maxiter=max(self.maxiter, 250),
+                       device=self.device, dipole_derivative=True)
+
+    def dipole_deriv(self, positions, chrg=0, spin=None, **_):
+        """Nuclear dipole derivative d mu / d R, (3, nat, 3) in e, by central
+        differences of the dipoles of the displaced single points that also
+        give the Hessian (``calculators/types/autograd.py:547-627``)."""
+        return self._hessian_dipole(positions, chrg, spin)[1]
+
+    def vibration(self, positions, chrg=0, spin=None, use_functorch=False,
+                  project_translational=True, project_rotational=True, **_):
+        """Harmonic vibrational analysis (``calculators/types/autograd.py:331-397``):
+        ``VibResult`` with frequencies (atomic units; ``use_common_units`` for
+        cm^-1) and normal modes (3 nat, nfreqs), from the GPU Hessian."""
+        from .properties import vib_analysis
+
+        hess = self.hessian(positions, chrg, spin)
+        return vib_analysis(self.numbers, positions, hess,
+                            project_translational=project_translational,
+                            project_rotational=project_rotational)
+
+    def ir(self, positions, chrg=0, spin=None, use_functorch=False, **_):
+        """IR spectrum (``calculators/types/autograd.py:941-993``): ``IRResult``
+        with frequencies and intensities (atomic units; ``use_common_units``
+        for cm^-1 and km/mol). The Hessian and the dipole derivative come from
+        one packed batch of the 6 nat displaced single points."""
+        from .properties import IRResult, ir_ints, vib_analysis
+
+        hess, dmu = self._hessian_dipole(positions, chrg, spin)
+        vib = vib_analysis(self.numbers, positions, hess)
+        return IRResult(vib.freqs, ir_ints(dmu, vib.modes))
+
     def singlepoint(self, positions, chrg=0, spin=None) -> Result:
         """The single point as a ``Result`` (calculators/types/energy.py:78-414)."""
         r = self._run(positions.detach(), chrg, spin)

@@ -25,13 +25,19 @@ from . import engine
 
 def hessian(tables, numbers, positions, *, h: float = 1e-3, chrg: float = 0.0, spin=None,
             etemp: float = 300.0, tol: float = 1e-10, maxiter: int = 250,
-            matrix: bool = False, device=None) -> torch.Tensor:
+            matrix: bool = False, device=None, dipole_derivative: bool = False):
     """
     Hessian (nat, 3, nat, 3) (or (3 nat, 3 nat) with ``matrix``) of one
     molecule in Eh/Bohr^2, float64, on the GPU. ``numbers`` (nat,) and
     ``positions`` (nat, 3) in Bohr; ``tables`` is the method's parameter set
     (``calculators.tables("gfn1" | "gfn2")``). Raises RuntimeError if any
     displaced single point fails or does not converge.
+
+    With ``dipole_derivative`` it returns ``(hessian, dmu_dr)``: the nuclear
+    derivative of the dipole moment, (3, nat, 3) in e (the reference's
+    ``dipole_deriv``, calculators/types/autograd.py:547-627), as central
+    differences of the dipole moments of the same displaced single points
+    (``dxtb_dipole_moment``, one launch for all of them).
     """
     z = np.asarray(numbers.cpu() if torch.is_tensor(numbers) else numbers, dtype=np.int64).ravel()
     z = z[z > 0]
@@ -58,4 +64,11 @@ def hessian(tables, numbers, positions, *, h: float = 1e-3, chrg: float = 0.0, s
     g = res.gradient.view(nd, nat * 3)  # packed: every molecule has nat atoms
     hmat = (g[0::2] - g[1::2]) / (2.0 * h)  # row (a, x): d g / d R_ax
     hmat = 0.5 * (hmat + hmat.T)
-    return hmat if matrix else hmat.view(nat, 3, nat, 3)
+    hout = hmat if matrix else hmat.view(nat, 3, nat, 3)
+    if not dipole_derivative:
+        return hout
+    from .properties import dipole_moments
+
+    mu = dipole_moments(pb, res.state["P"])  # (nd, 3)
+    dmu = ((mu[0::2] - mu[1::2]) / (2.0 * h)).T  # (3, 3 nat): d mu_x / d R_(a,y)
+    return hout, dmu.reshape(3, nat, 3)

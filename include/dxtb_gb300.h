@@ -234,6 +234,18 @@ int32_t dxtb_multipole_raw_vjp(const dxtb_batch *b, const double *par_f,
                                const double *grad_quadrupole, double *grad,
                                void *stream);
 
+/* Electric dipole moment of every molecule, dipole [nmol][3] in e a0:
+ * sum_A Z_A R_A - tr(P D0) (calculators/properties/moments/dip.py,
+ * dipole_xtb), with n0 [naos] the reference occupations (summing to the
+ * valence charge Z_A of each atom), density [mat] and dipole_origin
+ * [3][mat] the normalised dipole integrals about the origin from
+ * dxtb_multipole_raw. The reference's calculator obtains the same moment
+ * as dE/dF through its electric-field interaction (calculators/types/
+ * autograd.py:399-472, dipole). */
+int32_t dxtb_dipole_moment(const dxtb_batch *b, const double *n0,
+                           const double *density, const double *dipole_origin,
+                           double *dipole, void *stream);
+
 /* SCF workspace of one molecule in doubles (n AOs, nat atoms); the caller
  * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
 int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);

@@ -1044,6 +1044,24 @@ def gradient(sysm: System, positions, p, w, n0, solvation=None, exclude=()) -> t
     return g
 
 
+def dipole_moment(sysm: System, positions, p) -> torch.Tensor:
+    """
+    Electric dipole moment (e a0) at the density ``p``: the valence charges
+    at the nuclei minus the electronic moment about the origin,
+    sum_A Z_A R_A - tr(P D0) (``calculators/properties/moments/dip.py``
+    ``dipole_xtb``, with ``integral`` the normalised dipole integral about
+    the origin). Z_A = sum of the reference occupations of A's shells (the
+    neutral atom's valence electrons).
+    """
+    pos = torch.as_tensor(positions, dtype=DT)
+    s_raw = multipole_raw(sysm, pos, COMP_S)[0]
+    norm = snorm(s_raw)
+    d0 = multipole_raw(sysm, pos, COMP_D) * (norm[:, None] * norm[None, :])
+    n0, _ = reference_occupation(sysm, 0.0)
+    zval = torch.zeros(sysm.nat, dtype=DT).index_add_(0, torch.as_tensor(_orb_atom(sysm)), n0)
+    return (zval[:, None] * pos).sum(0) - torch.einsum("xij,ij->x", d0, p)
+
+
 # --------------------------------------------------------------------------
 # Turbomole ``coord`` reader (the format of test/test_singlepoint/mols/*/coord)
 # --------------------------------------------------------------------------

@@ -175,6 +175,16 @@ def main(ref_root: str) -> None:
     src["*/h0scale_gfn2"] = (
         "test/test_hamiltonian/test_gfn2.py ref (tblite 0.3.0): GFN2 H0 built with overlap=None"
     )
+    # GFN1 properties: dipole moment without field (e a0), harmonic
+    # frequencies (cm^-1) and IR intensities (km/mol)
+    props = _refs_dict((test / "test_properties" / "samples.py").read_text())
+    for m in ("H2", "LiH", "H2O", "CH4", "SiH4"):
+        for key in ("dipole", "freqs", "ints"):
+            g[f"props/{m}/{key}"] = props[m][key]
+    src["props/*"] = (
+        "test/test_properties/samples.py refs (GFN1): dipole (no field), freqs, ints; used by "
+        "test_dipole.py (atol 1e-3) and test_vibration_ref.py (atol 10 cm^-1, rtol 1e-3)"
+    )
     np.savez_compressed(HERE / "golden.npz", **g)
     (HERE / "golden_sources.json").write_text(json.dumps(src, indent=1))
 
