@@ -412,6 +412,8 @@ def main():
             "d2h_bytes_per_step": int(h_f.numel() * 8 + h_e.numel() * 8),
             "p50_ms": 1e3 * float(np.percentile(t_e2e, 50)),
             "p99_ms": 1e3 * float(np.percentile(t_e2e, 99)),
+            # repeated calls on the same molecules replay a captured CUDA graph
+            "cuda_graph_replay": bool(getattr(calc, "_graphs", None)),
         }
 
     # serving: the same molecules as a seeded Poisson request stream through the

@@ -63,6 +63,10 @@ _SIGS = {
     "dxtb_multipole_raw": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     "dxtb_multipole_raw_vjp": (i32, [vp] * 8),
     "dxtb_dipole_moment": (i32, [vp] * 6),
+    "dxtb_graph_begin": (i32, [vp]),
+    "dxtb_graph_end": (i32, [vp, vp]),
+    "dxtb_graph_launch": (i32, [vp, vp]),
+    "dxtb_graph_destroy": (i32, [vp]),
     "dxtb_scf_workspace_mol": (i64, [i64, i64]),
     "dxtb_scf": (i32, [vp] * 15 + [f64, vp] + [vp] * 17),
     "dxtb_gradient": (i32, [vp] * 22),

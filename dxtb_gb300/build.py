@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libdxtb_gb300.so"
 SOURCES = [
     "geometry.cu", "multipole.cu", "scf.cu", "gradient.cu", "indexmaps.cu", "solvation.cu",
-    "probe.cu", "properties.cu",
+    "probe.cu", "properties.cu", "graph.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]

@@ -34,6 +34,7 @@ drivers other than the PyTorch one (the GB300 kernels give its integrals).
 
 from __future__ import annotations
 
+import os
 import warnings
 
 import numpy as np
@@ -189,6 +190,7 @@ class Calculator:
                 radii.lookup(radii.VDW_D3, n, "van-der-Waals")
         self._pb: engine.PackedBatch | None = None
         self._pb_key = None
+        self._graphs: dict = {}  # CUDA graphs of the single point, by ``forces``
         self._state: dict = {}
         self._cache: dict = {}
 
@@ -295,17 +297,32 @@ class Calculator:
         spins = None if spin is None else self._chrg_list(spin, nmol)
         key = (tuple(chg), None if spins is None else tuple(spins))
         plist = [pos[i, : len(self._mols[i])] for i in range(nmol)]
+        kw = dict(etemp=self.etemp, maxiter=self.maxiter, tol=self.tol, forces=forces,
+                  gb=self.solvation, scf=self._scf)
         if self._pb is None or self._pb_key != key:
             self._pb = engine.PackedBatch(self.tables, self._mols, plist, self.device, chg,
                                           [int(s) for s in spins] if spins else None)
             self._pb_key = key
+            self._graphs = {}
             from . import autotune
 
             autotune.ensure(self._pb)  # large batches: the tuned size-class policy
+            res = engine.run(self._pb, state=self._state, **kw)
+        elif os.environ.get("DXTB_GRAPHS", "1") != "0":
+            # the same molecules again (a geometry optimisation, MD, or a
+            # repeated call): the second call captures the single point as a
+            # CUDA graph, later calls replay it with the new positions
+            g = self._graphs.get(forces)
+            if g is None:
+                self._pb.copy_positions_(plist)
+                g = engine.GraphStep(self._pb, **kw)
+                self._graphs[forces] = g
+                res = g.first
+            else:
+                res = g.replay(plist)
         else:
-            self._pb.set_positions(plist)
-        res = engine.run(self._pb, etemp=self.etemp, maxiter=self.maxiter, tol=self.tol,
-                         forces=forces, gb=self.solvation, state=self._state, scf=self._scf)
+            self._pb.copy_positions_(plist)
+            res = engine.run(self._pb, state=self._state, **kw)
         st = res.status.cpu()
         bad = st[(st != 0)]
         if len(bad):

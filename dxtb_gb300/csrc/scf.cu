@@ -879,6 +879,7 @@ struct SideStream {
   cudaStream_t caller = nullptr;
   cudaStream_t s[kClasses] = {};
   cudaEvent_t fork = nullptr, join[kClasses] = {};
+  int prio[kClasses] = {};  // priority of s[c], also set on each class launch
   bool used = false;
 };
 constexpr int kSidePerDev = 32;
@@ -916,6 +917,7 @@ static int32_t side_stream(cudaStream_t caller, SideStream **out) {
     const int prio = cprio != least ? cprio : max(greatest, least - c);  // class 0: the lowest
     if (cudaStreamCreateWithPriority(&slot->s[c], cudaStreamNonBlocking, prio) != cudaSuccess)
       return DXTB_ERR_LAUNCH;
+    slot->prio[c] = prio;
     if (cudaEventCreateWithFlags(&slot->join[c], cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
   }
   if (cudaEventCreateWithFlags(&slot->fork, cudaEventDisableTiming) != cudaSuccess) return DXTB_ERR_LAUNCH;
@@ -1043,28 +1045,43 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     cfg.blockDim = dim3(kScfBigThreads);
     cfg.dynamicSmemBytes = class_smem(c);
     cfg.stream = ss ? ss->s[c] : st;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = csize;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    // the class stream's priority, set on the launch as well so that a
+    // captured graph keeps it as a node priority (dxtb_graph_end)
+    at[1].id = cudaLaunchAttributePriority;
+    at[1].val.priority = ss ? ss->prio[c] : 0;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = ss ? 2 : 1;
     if (cudaLaunchKernelEx(&cfg, k_scf_cluster, a, c) != cudaSuccess) return DXTB_ERR_LAUNCH;
     const int32_t rc = class_gradient(a, g, c, cfg.stream);
     if (rc != DXTB_OK) return rc;
   }
+  // one-SM and shared-SM classes, likewise with their stream's priority
+  auto launch_cta_class = [&](auto kernel, int c, int threads, size_t dyn) -> int32_t {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nmol);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = dyn;
+    cfg.stream = ss ? ss->s[c] : st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = ss ? ss->prio[c] : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = ss ? 1 : 0;
+    if (cudaLaunchKernelEx(&cfg, kernel, a, c) != cudaSuccess) return DXTB_ERR_LAUNCH;
+    return class_gradient(a, g, c, cfg.stream);
+  };
   if (cmax >= 1) {
-    k_scf<kScfBigThreads, 1><<<nmol, kScfBigThreads, class_smem(1), ss ? ss->s[1] : st>>>(a, 1);
-    DXTB_CHECK_LAUNCH();
-    const int32_t rc = class_gradient(a, g, 1, ss ? ss->s[1] : st);
+    const int32_t rc = launch_cta_class(k_scf<kScfBigThreads, 1>, 1, kScfBigThreads, class_smem(1));
     if (rc != DXTB_OK) return rc;
   }
   const size_t smem0 = (size_t)min(nmax, a.thr[1]) * (3 * sizeof(double) + 2 * sizeof(float));
-  k_scf<kScfThreads, 2><<<nmol, kScfThreads, smem0, ss ? ss->s[0] : st>>>(a, 0);
-  DXTB_CHECK_LAUNCH();
   {
-    const int32_t rc = class_gradient(a, g, 0, ss ? ss->s[0] : st);
+    const int32_t rc = launch_cta_class(k_scf<kScfThreads, 2>, 0, kScfThreads, smem0);
     if (rc != DXTB_OK) return rc;
   }
   if (ss) {

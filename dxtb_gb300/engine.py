@@ -137,6 +137,13 @@ class PackedBatch:
         self.positions = torch.cat([p.to(self.device) for p in pos]).contiguous()
         self._struct = None
 
+    def copy_positions_(self, positions: list) -> None:
+        """Overwrite the device positions in place (same molecules), keeping
+        their address: a captured ``GraphStep`` reads them from there."""
+        pos = [torch.as_tensor(p, dtype=F64).reshape(-1, 3)[: int(self.nat[i])].to(self.device)
+               for i, p in enumerate(positions)]
+        self.positions.copy_(torch.cat(pos))
+
     @property
     def struct(self) -> _lib.Batch:
         if self._struct is None:
@@ -236,12 +243,14 @@ def scf_config(maxiter: int, tol: float, scf: dict | None = None) -> _lib.ScfCon
 
 def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float = 1e-10,
         forces: bool = False, gb: dict | None = None, state: dict | None = None,
-        events: dict | None = None, scf: dict | None = None) -> Result:
+        events: dict | None = None, scf: dict | None = None, collect: bool = True) -> Result:
     """
     One single point for every molecule of the packed batch. With ``events``
     (a dict), CUDA events are recorded on the current stream around each
     stage: events[stage] = (start, end). ``scf`` selects the root solver
-    and its tolerances (``scf_config``).
+    and its tolerances (``scf_config``). With ``collect=False`` only the
+    library's kernels are launched (no PyTorch operation allocates) and the
+    number of launches is returned; ``collect_result`` then reads the state.
     """
     L = _lib.lib()
 
@@ -353,8 +362,6 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
         _lib.check(L.dxtb_scf(*scf_args, st), "SCF")
         launches += n_scf
         mark("scf", 1)
-    e4 = en[: 4 * pb.nmol].view(pb.nmol, 4)
-    e_rep = _seg_sum(erep[:na], pb.t["atom_mol"], pb.nmol)
     if forces:
         mark("gradient", 0)
         if gb is not None:
@@ -365,6 +372,82 @@ def run(pb: PackedBatch, *, etemp: float = 300.0, maxiter: int = 250, tol: float
             )
             launches += 1
         mark("gradient", 1)
-        grad = grad[: 3 * na].view(na, 3)
+    if not collect:
+        return launches
+    return collect_result(pb, s, forces, launches)
+
+
+def collect_result(pb: PackedBatch, s: dict, forces: bool, launches: int = 0) -> Result:
+    """The per-molecule results of a single point from its state buffers."""
+    na = pb.total["atoms"]
+    e4 = s["energies"][: 4 * pb.nmol].view(pb.nmol, 4)
+    e_rep = _seg_sum(s["erep"][:na], pb.t["atom_mol"], pb.nmol)
+    grad = s["grad"][: 3 * na].view(na, 3) if forces else None
     energy = e4[:, 0] + e4[:, 1] + e_rep
-    return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], status[: pb.nmol], grad, s, launches)
+    return Result(energy, e4[:, 0], e4[:, 1], e_rep, e4[:, 2], s["status"][: pb.nmol], grad, s,
+                  launches)
+
+
+
+class GraphStep:
+    """
+    The single point of one fixed packed batch as a CUDA graph: the geometry
+    kernels, the integrals, the per-class SCF (and gradient) launches on
+    their forked streams and the joins, captured once through the library's
+    ``dxtb_graph_*`` entry points and replayed for new positions of the same
+    molecules (geometry optimisation, molecular dynamics, repeated calls of
+    a calculator). The graph keeps the SCF's class priorities as node
+    priorities.
+
+    The constructor runs the step once eagerly on a dedicated stream (this
+    allocates the state and creates the library's per-stream class streams,
+    none of which may happen inside a capture), keeps that result as
+    ``first``, and then captures the launches on the same stream.
+    ``replay`` copies new positions into the batch's device buffer in place,
+    launches the graph and collects the results from the state buffers (a
+    few PyTorch reductions, outside the graph). ``run_kw`` are the keyword
+    arguments of ``run`` other than ``state``, ``events`` and ``collect``.
+    """
+
+    def __init__(self, pb: PackedBatch, **run_kw):
+        self.pb = pb
+        self.kw = run_kw
+        self.state: dict = {}
+        self.exec = None
+        L = _lib.lib()
+        self.stream = torch.cuda.Stream(device=pb.device)
+        cur = torch.cuda.current_stream(pb.device)
+        self.stream.wait_stream(cur)
+        with torch.cuda.stream(self.stream):
+            self.first = run(pb, state=self.state, **run_kw)
+            self.launches = self.first.launches
+            sp = C.c_void_p(self.stream.cuda_stream)
+            _lib.check(L.dxtb_graph_begin(sp), "graph capture")
+            try:
+                run(pb, state=self.state, collect=False, **run_kw)
+            finally:
+                ex = C.c_void_p()
+                rc = L.dxtb_graph_end(sp, C.byref(ex))
+            _lib.check(rc, "graph instantiation")
+            self.exec = ex
+        cur.wait_stream(self.stream)
+
+    def replay(self, positions: list | None = None) -> Result:
+        cur = torch.cuda.current_stream(self.pb.device)
+        if positions is not None:
+            self.pb.copy_positions_(positions)
+        self.stream.wait_stream(cur)
+        with torch.cuda.stream(self.stream):
+            _lib.check(_lib.lib().dxtb_graph_launch(self.exec, C.c_void_p(self.stream.cuda_stream)),
+                       "graph launch")
+            res = collect_result(self.pb, self.state, bool(self.kw.get("forces", False)), self.launches)
+        cur.wait_stream(self.stream)
+        return res
+
+    def __del__(self):
+        if getattr(self, "exec", None) is not None and _lib is not None:
+            try:
+                _lib.lib().dxtb_graph_destroy(self.exec)
+            except Exception:
+                pass
+            self.exec = None

@@ -51,9 +51,11 @@ def dipole_moments(pb, density: torch.Tensor, stream=None) -> torch.Tensor:
     out = torch.empty(pb.nmol * 3, dtype=torch.float64, device=dev)
     st = _lib.stream_ptr() if stream is None else stream
     _lib.check(L.dxtb_multipole_raw(C.byref(pb.struct), pb.t["par_f"].data_ptr(),
-                                    pb.t["par_i"].data_ptr(), s.data_ptr(), d0.data_ptr(), None, st))
+                                    pb.t["par_i"].data_ptr(), s.data_ptr(), d0.data_ptr(), None, st),
+               "dipole integrals")
     _lib.check(L.dxtb_dipole_moment(C.byref(pb.struct), pb.t["n0"].data_ptr(), density.data_ptr(),
-                                    d0.data_ptr(), out.data_ptr(), st))
+                                    d0.data_ptr(), out.data_ptr(), st),
+               "dipole moment")
     return out.view(pb.nmol, 3)
 
 

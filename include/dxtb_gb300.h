@@ -246,6 +246,23 @@ int32_t dxtb_dipole_moment(const dxtb_batch *b, const double *n0,
                            const double *density, const double *dipole_origin,
                            double *dipole, void *stream);
 
+/* CUDA graph of a sequence of this library's calls on one stream (the
+ * reference has no counterpart: it re-dispatches its PyTorch operators on
+ * every call). dxtb_graph_begin starts a thread-local capture on `stream`
+ * (not the legacy default stream); the entry points called on it
+ * afterwards, with the same buffers, are recorded instead of run, including
+ * the work dxtb_scf/dxtb_scf_gradient fork onto their per-class streams.
+ * Their first call on `stream` must come before the capture (it creates
+ * those streams and sets per-device kernel attributes). dxtb_graph_end ends
+ * the capture and returns an executable graph in *exec, instantiated with
+ * node priorities so the SCF's class priorities hold on replay.
+ * dxtb_graph_launch replays it on a stream; dxtb_graph_destroy frees it.
+ * Replays read and write the buffers given at capture time. */
+int32_t dxtb_graph_begin(void *stream);
+int32_t dxtb_graph_end(void *stream, void **exec);
+int32_t dxtb_graph_launch(void *exec, void *stream);
+int32_t dxtb_graph_destroy(void *exec);
+
 /* SCF workspace of one molecule in doubles (n AOs, nat atoms); the caller
  * lays the molecules' workspaces out at ws_off[m] (prefix of these sizes). */
 int64_t dxtb_scf_workspace_mol(int64_t n, int64_t nat);

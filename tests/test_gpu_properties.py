@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 G = np.load(Path(__file__).parent / "golden" / "golden.npz")
 OPTS = {"scf_mode": "full", "mixer": "anderson", "maxiter": 100, "x_atol": 1e-10,
-        "f_atol": 1e-10, "exclude": ["disp", "d4sc"]}
+        "f_atol": 1e-10, "guess": "sad", "exclude": ["disp", "d4sc"]}
 
 
 def calc(method, name):
