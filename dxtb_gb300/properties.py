@@ -48,10 +48,12 @@ def dipole_moments(pb, density: torch.Tensor, stream=None) -> torch.Tensor:
     dev = pb.device
     s = torch.empty(nm, dtype=torch.float64, device=dev)
     d0 = torch.empty(3 * nm, dtype=torch.float64, device=dev)
+    q9 = torch.empty(9 * nm, dtype=torch.float64, device=dev)  # the kernel writes D and Q together
     out = torch.empty(pb.nmol * 3, dtype=torch.float64, device=dev)
     st = _lib.stream_ptr() if stream is None else stream
     _lib.check(L.dxtb_multipole_raw(C.byref(pb.struct), pb.t["par_f"].data_ptr(),
-                                    pb.t["par_i"].data_ptr(), s.data_ptr(), d0.data_ptr(), None, st),
+                                    pb.t["par_i"].data_ptr(), s.data_ptr(), d0.data_ptr(),
+                                    q9.data_ptr(), st),
                "dipole integrals")
     _lib.check(L.dxtb_dipole_moment(C.byref(pb.struct), pb.t["n0"].data_ptr(), density.data_ptr(),
                                     d0.data_ptr(), out.data_ptr(), st),

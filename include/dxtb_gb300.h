@@ -189,7 +189,8 @@ int32_t dxtb_multipole_h0(const dxtb_batch *b, const double *par_f,
 /* Raw multipole integrals about the origin as returned by the integral
  * wrappers overlap/dipint/quadint (integral/wrappers.py:149-315):
  * overlap [mat], dipole [3][mat], quadrupole [9][mat] (row-major xx..zz),
- * all normalised, not shifted, not made traceless. */
+ * all normalised, not shifted, not made traceless. The moments are written
+ * together: with dipole or quadrupole null, only the overlap is. */
 int32_t dxtb_multipole_raw(const dxtb_batch *b, const double *par_f,
                            const int32_t *par_i, double *overlap,
                            double *dipole, double *quadrupole, void *stream);
