@@ -102,14 +102,17 @@ class Server:
     is queued. With ``order="size"`` each lane admits its smallest request
     first, and a pack takes only requests of at most twice its head's size
     (shortest job first: the percentiles of a burst of mixed sizes drop, the
-    largest requests finish last).
+    largest requests finish last). ``large_order`` overrides the order of
+    the large lane; "longest" admits its largest request first, with pack
+    members of at least half its size (the longest job starts first, which
+    shortens the makespan of a burst, and with it the tail latency).
     """
 
     LANES = ("large", "small")
 
     def __init__(self, executor, *, hbm_budget: float = 120e9, slots: int = 8, max_pack: int = 32,
                  large_slots: int = 0, large_n: int | None = None, large_pack: int = 4,
-                 order: str = "fifo", clock=time.perf_counter):
+                 order: str = "fifo", large_order: str | None = None, clock=time.perf_counter):
         if slots < 1 or max_pack < 1 or large_pack < 1:
             raise ValueError("slots and pack sizes must be positive")
         if not 0 <= large_slots < slots:
@@ -125,7 +128,10 @@ class Server:
         self.large_pack = large_pack
         if order not in ("fifo", "size"):
             raise ValueError("order is 'fifo' or 'size'")
+        if large_order not in (None, "fifo", "size", "longest"):
+            raise ValueError("large_order is 'fifo', 'size' or 'longest'")
         self.order = order
+        self.lane_order = {"small": order, "large": large_order or order}
         self._sizes: dict[int, int] = {}
         self.clock = clock
         self.t0 = clock()
@@ -209,9 +215,15 @@ class Server:
                 q = self.queues[lane]
                 if not q:
                     continue
-                if self.order == "size":
+                order = self.lane_order[lane]
+                if order == "size":
                     # shortest first (stable: arrival order among equal sizes)
                     q = deque(sorted(q, key=self._size))
+                    self.queues[lane] = q
+                elif order == "longest":
+                    # longest first: the makespan of a burst of large
+                    # requests is set by the longest, so it starts first
+                    q = deque(sorted(q, key=lambda r: -self._size(r)))
                     self.queues[lane] = q
                 if not self.free[lane] and not (lane == "small" and not self.queues["large"]
                                                 and self.free["large"]):
@@ -236,7 +248,8 @@ class Server:
                 while q:
                     r = q.popleft()
                     if (len(take) < cap and r.method == head.method
-                            and (self.order != "size" or self._size(r) <= 2 * nhead)):
+                            and (order != "size" or self._size(r) <= 2 * nhead)
+                            and (order != "longest" or 2 * self._size(r) >= nhead)):
                         b = nb if r is head else self.ex.nbytes(r)
                         if tot + b <= free:
                             take.append(r)

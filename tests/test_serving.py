@@ -152,6 +152,28 @@ def test_size_order_packs_similar_sizes_smallest_first():
     assert order[1:] == [[4, 2, 0], [5]]  # head 25 atoms (50 orbitals): up to 100 join
 
 
+def test_longest_first_large_lane():
+    """large_order="longest": the large lane admits its largest request
+    first, with pack members of at least half its size; the small lane keeps
+    its own order."""
+    clk = FakeClock()
+    ex = FakeExecutor(clk)
+    srv = Server(ex, hbm_budget=1e12, slots=2, max_pack=8, large_slots=1, large_n=200,
+                 large_pack=2, order="size", large_order="longest", clock=clk)
+    for rid, nat in enumerate([120, 300, 100, 160, 10, 5]):
+        srv.submit(_req(rid, nat=nat))
+    srv.pump()
+    # large lane (>= 100 atoms): 300 first, then 160 (>= 150) joins; 120 and 100 wait
+    assert ex.launched[0] == ([1, 3], 1, 0.0)
+    assert ex.launched[1][0] == [5, 4]  # small lane: smallest first
+    while not srv.idle:
+        srv.pump()
+        clk.t += 0.05
+    assert [ids for ids, slot, _ in ex.launched if slot == 1][1] == [0, 2]
+    with pytest.raises(ValueError):
+        Server(ex, large_order="random")
+
+
 def test_small_requests_borrow_idle_large_slots():
     clk = FakeClock()
     ex = FakeExecutor(clk)
