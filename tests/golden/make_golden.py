@@ -185,6 +185,26 @@ def main(ref_root: str) -> None:
         "test/test_properties/samples.py refs (GFN1): dipole (no field), freqs, ints; used by "
         "test_dipole.py (atol 1e-3) and test_vibration_ref.py (atol 10 cm^-1, rtol 1e-3)"
     )
+    # SCF energies of multi-atom molecules (E_scf - TS): GFN1 from tblite
+    # 0.2.1 with repulsion and dispersion disabled; GFN2 from tblite 0.4.0
+    # ("electronic energy", which holds the self-consistent D4 part)
+    scf = _refs_dict((test / "test_scf" / "samples.py").read_text())
+    for m in ("H2", "LiH", "H2O", "CH4", "SiH4", "MB16_43_01", "LYS_xao"):
+        for key in ("egfn1", "egfn2"):
+            g[f"scf/{m}/{key}"] = scf[m][key]
+    chg = _refs_dict((test / "test_scf" / "samples_charged.py").read_text())
+    num, pos = _coord(test / "test_singlepoint" / "mols" / "AD7en+" / "coord", symbols)
+    g["AD7en+/numbers"] = num
+    g["AD7en+/positions"] = pos
+    for key in ("charge", "egfn1", "egfn2"):
+        g[f"scf/AD7en+/{key}"] = chg["AD7en+"][key]
+    src["scf/*"] = (
+        "test/test_scf/samples.py and samples_charged.py (AD7en+, charge +1): egfn1 (tblite "
+        "0.2.1, repulsion and dispersion disabled), egfn2 (tblite 0.4.0 electronic energy, with "
+        "the self-consistent D4 part); used by test_scf.py / test_charged.py with "
+        "tol sqrt(eps) * 10"
+    )
+    src["AD7en+/*"] = "test/test_singlepoint/mols/AD7en+/coord"
     np.savez_compressed(HERE / "golden.npz", **g)
     (HERE / "golden_sources.json").write_text(json.dumps(src, indent=1))
 

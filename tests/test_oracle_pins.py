@@ -195,3 +195,20 @@ def test_anderson_loop_reaches_the_pinned_solution(method):
     assert abs(tight.energy - ref.energy) < 1e-10
     assert abs(loose.energy - ref.energy) < 1e-6
     assert loose.iterations < tight.iterations
+
+
+SCF_MOLS = ["H2", "LiH", "H2O", "CH4", "SiH4", "MB16_43_01", "LYS_xao", "AD7en+"]
+
+
+@pytest.mark.parametrize("name", SCF_MOLS)
+def test_gfn1_scf_energies(name):
+    """test/test_scf/samples.py and samples_charged.py (tblite 0.2.1,
+    repulsion and dispersion disabled; AD7en+ is a cation): the whole GFN1
+    SCF of multi-atom molecules, E_scf - TS, at the reference test's
+    tolerance sqrt(eps) * 10. (The GFN2 values of the same files are tblite's
+    electronic energy with its self-consistent D4 part, which this path
+    excludes; they are not pins here.)"""
+    num, pos = mol(name)
+    chrg = float(G[f"scf/{name}/charge"]) if f"scf/{name}/charge" in G.files else 0.0
+    r = X.singlepoint("gfn1", num, pos, chrg=chrg, tol=1e-10, maxiter=250, exclude=("rep",))
+    assert abs(r.energy - float(G[f"scf/{name}/egfn1"])) < np.sqrt(np.finfo(np.float64).eps) * 10
