@@ -34,13 +34,23 @@ def _prefix(v: np.ndarray) -> np.ndarray:
 
 
 def alpha_beta(nel: float, spin: int | None = None) -> tuple[float, float]:
-    """Alpha/beta electrons (wavefunction/filling.py:180-259)."""
+    """
+    Alpha/beta electrons (wavefunction/filling.py:180-259): ``spin`` unpaired
+    electrons, or the parity of the rounded electron count when None. As in
+    the reference, more unpaired electrons than electrons, or a parity that
+    does not match the electron count, raise ValueError.
+    """
+    parity = math.floor(nel + 0.5) % 2
     if spin is None:
-        uhf = math.floor(nel + 0.5) % 2
+        uhf = parity
     else:
         uhf = int(spin)
-        if uhf % 2 != math.floor(nel + 0.5) % 2:
-            uhf = math.floor(nel + 0.5) % 2
+        if uhf > math.floor(nel + 0.5):
+            raise ValueError(f"Number of unpaired electrons ({uhf}) larger than "
+                             f"number of electrons ({nel}).")
+        if uhf % 2 != parity:
+            raise ValueError(f"Odd (even) number of unpaired electrons ({uhf}) but even "
+                             f"(odd) number of electrons ({nel}) given.")
     diff = min(uhf, nel)
     nb = (nel - diff) / 2.0
     return nb + diff, nb

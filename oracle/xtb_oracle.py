@@ -731,14 +731,20 @@ def repulsion_energy(sysm: System, positions) -> torch.Tensor:
 # --------------------------------------------------------------------------
 
 
-def reference_occupation(sysm: System, chrg: float = 0.0):
-    """``scf/iterator.py:147-195`` and ``filling.py:180-259`` (spin=None)."""
+def reference_occupation(sysm: System, chrg: float = 0.0, spin: int | None = None):
+    """``scf/iterator.py:147-195`` and ``filling.py:180-259``: ``spin``
+    unpaired electrons (None: the parity of the electron count); a count
+    above the electrons or of the wrong parity raises ValueError."""
     sp = shell_params(sysm)
     nsph = torch.as_tensor(sysm.ih["orbitals_per_shell"]).to(DT)
     o2s = torch.as_tensor(sysm.ih["orbitals_to_shell"])
     n0 = (sp["refocc"] / nsph)[o2s]
     nel = float(sp["refocc"].sum()) - chrg
     uhf = math.floor(nel + 0.5) % 2
+    if spin is not None:
+        if spin > math.floor(nel + 0.5) or spin % 2 != uhf:
+            raise ValueError(f"{spin} unpaired electrons do not fit {nel} electrons")
+        uhf = int(spin)
     diff = min(uhf, nel)
     nb = (nel - diff) / 2.0
     return n0, (nb + diff, nb)
@@ -844,6 +850,7 @@ def singlepoint(
     numbers,
     positions,
     chrg: float = 0.0,
+    spin: int | None = None,
     etemp: float = 300.0,
     maxiter: int = 250,
     tol: float = 1e-11,
@@ -870,7 +877,7 @@ def singlepoint(
     kt = etemp * _radii.KELVIN2AU
     with torch.no_grad():
         s, d, q, h0, cn, c = _geometry_terms(sysm, pos, solvation)
-        n0, (na, nb) = reference_occupation(sysm, chrg)
+        n0, (na, nb) = reference_occupation(sysm, chrg, spin)
         lchol = torch.linalg.cholesky(s)
         linv = torch.linalg.inv(lchol)
         nat = sysm.nat

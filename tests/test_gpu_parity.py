@@ -41,6 +41,32 @@ def test_energy_forces_fixture_molecules(method, name):
 
 
 @pytest.mark.parametrize("method", ["gfn1", "gfn2"])
+def test_charges_and_spin_states(method):
+    """Cations, anions and high-spin states in one packed batch: alpha and
+    beta electrons from the charge and the number of unpaired electrons
+    (wavefunction/filling.py:180-259), separate Fermi occupations per
+    channel, against the oracle with the same charge and spin."""
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.workloads import random_molecule
+
+    # (atoms, charge, unpaired electrons); the neutral molecules have even
+    # electron counts, so a charge of +-1 needs an odd spin
+    cases = [(12, 0.0, 2), (18, 1.0, 1), (25, -1.0, 3), (30, 2.0, 0), (16, 0.0, 4)]
+    mols = [random_molecule(2600 + i, n) for i, (n, _, _) in enumerate(cases)]
+    pb = PackedBatch(tables(method), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols],
+                     charges=[c for _, c, _ in cases], spins=[s for _, _, s in cases])
+    res = run(pb, forces=True, tol=1e-10, maxiter=250)
+    assert (res.status.cpu() == 0).all()
+    g = res.gradient.cpu().numpy()
+    for i, ((num, pos), (_, chrg, spin)) in enumerate(zip(mols, cases)):
+        ref = X.singlepoint(method, num, pos, chrg=chrg, spin=spin, grad=True, tol=1e-12)
+        assert abs(float(res.energy[i]) - ref.energy) < E_TOL, i
+        gi = g[pb.atom_off[i] : pb.atom_off[i + 1]]
+        assert np.abs(gi - ref.extra["gradient"].numpy()).max() < F_TOL, i
+
+
+@pytest.mark.parametrize("method", ["gfn1", "gfn2"])
 def test_batch_of_synthetic_molecules(method):
     from dxtb_gb300.engine import PackedBatch, run
     from dxtb_gb300.calculators import tables

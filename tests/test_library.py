@@ -131,3 +131,17 @@ def test_scf_workspace_grows_with_size():
     assert 0 < a < b
     # at least the three n x n matrices of the molecule
     assert a >= 3 * 90 * 90 and b >= 3 * 172 * 172
+
+
+def test_alpha_beta_split_and_errors():
+    """Alpha/beta electrons as in wavefunction/filling.py:180-259, with its
+    ValueErrors for too many unpaired electrons and a wrong parity."""
+    from dxtb_gb300.engine import alpha_beta
+
+    assert alpha_beta(10.0) == (5.0, 5.0)
+    assert alpha_beta(9.0) == (5.0, 4.0)
+    assert alpha_beta(10.0, 2) == (6.0, 4.0)
+    assert alpha_beta(9.0, 3) == (6.0, 3.0)
+    for nel, spin in [(10.0, 1), (9.0, 2), (2.0, 4)]:
+        with pytest.raises(ValueError):
+            alpha_beta(nel, spin)
