@@ -72,6 +72,7 @@ class _Pack:
     nbytes: int
     admitted: float
     handle: object = None
+    sms: int = 0  # SMs counted against the large lane's cap
 
 
 @dataclass
@@ -99,7 +100,11 @@ class Server:
     ``large_pack``. A pack returns when its slowest member is done, so small
     requests would otherwise wait for the largest molecule admitted with
     them. Small requests may use an idle large slot while no large request
-    is queued. With ``order="size"`` each lane admits its smallest request
+    is queued. ``large_sms`` caps the SMs that in-flight large packs hold
+    (``executor.team_sms(req)`` per molecule): the SCF kernels are persistent
+    and keep their SMs until the molecule converges, so without a cap the
+    large molecules' clusters can occupy every SM for seconds while small
+    requests wait. With ``order="size"`` each lane admits its smallest request
     first, and a pack takes only requests of at most twice its head's size
     (shortest job first: the percentiles of a burst of mixed sizes drop, the
     largest requests finish last). ``large_order`` overrides the order of
@@ -112,7 +117,8 @@ class Server:
 
     def __init__(self, executor, *, hbm_budget: float = 120e9, slots: int = 8, max_pack: int = 32,
                  large_slots: int = 0, large_n: int | None = None, large_pack: int = 4,
-                 order: str = "fifo", large_order: str | None = None, clock=time.perf_counter):
+                 order: str = "fifo", large_order: str | None = None,
+                 large_sms: int | None = None, clock=time.perf_counter):
         if slots < 1 or max_pack < 1 or large_pack < 1:
             raise ValueError("slots and pack sizes must be positive")
         if not 0 <= large_slots < slots:
@@ -132,7 +138,10 @@ class Server:
             raise ValueError("large_order is 'fifo', 'size' or 'longest'")
         self.order = order
         self.lane_order = {"small": order, "large": large_order or order}
+        self.large_sms = large_sms
+        self.sms_used = 0  # SMs held by in-flight large packs
         self._sizes: dict[int, int] = {}
+        self._teams: dict[int, int] = {}
         self.clock = clock
         self.t0 = clock()
         self.queues = {"small": deque(), "large": deque()}
@@ -162,6 +171,14 @@ class Server:
             n = self.ex.norb(req) if hasattr(self.ex, "norb") else len(req.numbers)
             self._sizes[id(req)] = n
         return n
+
+    def _team_sms(self, req: Request) -> int:
+        """SMs of a request's SCF team (cached), counted against ``large_sms``."""
+        t = self._teams.get(id(req))
+        if t is None:
+            t = self.ex.team_sms(req) if hasattr(self.ex, "team_sms") else 1
+            self._teams[id(req)] = t
+        return t
 
     def lane(self, req: Request) -> str:
         if self.large_slots > 0 and self._size(req) >= self.large_n:
@@ -194,6 +211,7 @@ class Server:
                 out.append(Response(r.rid, float(e), f, int(it), int(st), r.arrival, pk.admitted, t,
                                     pk.pid, len(pk.requests)))
             self.used -= pk.nbytes
+            self.sms_used -= pk.sms
             self.free[self._slot_lane(pk.slot)].append(pk.slot)
             pk.handle = None
         self.inflight = keep
@@ -229,6 +247,20 @@ class Server:
                                                 and self.free["large"]):
                     continue
                 head = q[0]
+                capped = lane == "large" and self.large_sms is not None
+                sms_free = (self.large_sms - self.sms_used) if capped else 0
+                if capped:
+                    if self.sms_used == 0:
+                        # a molecule whose team alone exceeds the cap still runs
+                        sms_free = max(sms_free, self._team_sms(head))
+                    # backfill: the first queued request whose team fits leads
+                    fit = next((r for r in q if self._team_sms(r) <= sms_free), None)
+                    if fit is None:
+                        continue  # wait for the large lane's SMs
+                    if fit is not head:
+                        q = deque([fit] + [r for r in q if r is not fit])
+                        self.queues[lane] = q
+                        head = fit
                 free = self.budget - self.used
                 nb = self.ex.nbytes(head)
                 if nb > self.budget:
@@ -244,21 +276,24 @@ class Server:
                     continue  # wait for memory: in-flight packs will release it
                 cap = self.large_pack if lane == "large" else self.max_pack
                 nhead = self._size(head)
-                take, rest, tot = [], deque(), 0
+                take, rest, tot, sms = [], deque(), 0, 0
                 while q:
                     r = q.popleft()
                     if (len(take) < cap and r.method == head.method
                             and (order != "size" or self._size(r) <= 2 * nhead)
                             and (order != "longest" or 2 * self._size(r) >= nhead)):
                         b = nb if r is head else self.ex.nbytes(r)
-                        if tot + b <= free:
+                        t = self._team_sms(r) if capped else 0
+                        if tot + b <= free and (not capped or sms + t <= sms_free):
                             take.append(r)
                             tot += b
+                            sms += t
                             continue
                     rest.append(r)
                 self.queues[lane] = rest
                 slot = self._take_slot(lane)
-                pk = _Pack(self._pid, slot, take, tot, self.now())
+                pk = _Pack(self._pid, slot, take, tot, self.now(), sms=sms)
+                self.sms_used += sms
                 self._pid += 1
                 pk.handle = self.ex.launch(take, slot)
                 self.inflight.append(pk)
@@ -375,6 +410,20 @@ class CudaExecutor:
     def norb(self, req: Request) -> int:
         """Orbitals of the request's molecule."""
         return self._sizes(req)[0]
+
+    def team_sms(self, req: Request) -> int:
+        """SMs the request's SCF holds while it runs: 1 for the one-CTA size
+        classes, the cluster size (2-16) for the others (the size-class
+        policy of the library)."""
+        import ctypes as C
+
+        from . import _lib
+
+        thr = (C.c_int32 * 5)()
+        _lib.check(_lib.lib().dxtb_scf_get_size_classes(thr), "size classes")
+        n = self.norb(req)
+        c = sum(1 for t in thr if n >= t)  # size class 0..5
+        return 1 if c <= 1 else 1 << (c - 1)
 
     def nbytes(self, req: Request) -> int:
         """Device bytes of one request's state (integrals, caches, SCF workspace, outputs)."""
