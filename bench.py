@@ -53,6 +53,8 @@ def args():
     p.add_argument("--serve-rate", type=float, default=2000.0,
                    help="Poisson arrival rate of the serving leg (0: skip the leg)")
     p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the config-1 latency and config-3 throughput legs")
     p.add_argument("--config4", action="store_true",
                    help="also run the serving configuration: 200 Poisson requests at 2000/s, "
                         "GFN1/GFN2, 8-300 atoms log-uniform, E+F, 120 GB budget")
@@ -274,6 +276,74 @@ def set_parity(res, pb) -> dict:
     }
 
 
+def other_configs(dev, steps: int) -> dict:
+    """Config 1: GFN1 E+F of C8N2O2H12 (24 atoms, n = 72) through
+    GFN1Calculator, latency per call (repeated calls replay the CUDA graph),
+    positions from the host. Config 3: the 64 molecules of 30-120 atoms as
+    one packed batch per method, E+F, device-resident, CUDA events; every
+    molecule against the oracle fixture (tests/golden/sets_c3.npz), with the
+    GFN1 molecules whose oracle SCF needs over 100 iterations counted apart."""
+    from dxtb_gb300 import GFN1Calculator
+    from dxtb_gb300.calculators import tables
+    from dxtb_gb300.engine import PackedBatch, run
+    from dxtb_gb300.workloads import config_molecules
+
+    out = {}
+    z1, p1 = config_molecules(1)[0]
+    calc = GFN1Calculator(torch.as_tensor(z1), opts={
+        "scf_mode": "implicit", "x_atol": 1e-10, "f_atol": 1e-10, "maxiter": 250,
+        "guess": "sad", "exclude": ["disp", "d4sc"]}, device=dev)
+    hp = torch.tensor(p1).pin_memory()
+    lat = []
+    for k in range(3 + max(steps, 5)):
+        calc.reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f = calc.get_forces(hp.to(dev, non_blocking=True)).cpu()
+        e = float(calc.get_energy(hp.to(dev, non_blocking=True)))
+        lat.append(time.perf_counter() - t0)
+    lat = lat[3:]
+    out["config1"] = {
+        "workload": "GFN1 E+F, C8N2O2H12 (24 atoms, n = 72), seed 1000, through GFN1Calculator",
+        "p50_ms": 1e3 * float(np.median(lat)), "min_ms": 1e3 * float(min(lat)),
+        "energy": e, "cuda_graph_replay": bool(calc._graphs),
+    }
+    d = np.load(ROOT / "tests" / "golden" / "sets_c3.npz")
+    nat = d["nat"]
+    nums = [d["numbers"][i, : nat[i]] for i in range(len(nat))]
+    pos = [torch.tensor(d["positions"][i, : nat[i]]) for i in range(len(nat))]
+    chaotic = {"gfn1": {1, 6, 23, 37, 48, 53}, "gfn2": set()}  # oracle > 100 iterations
+    for method in ("gfn1", "gfn2"):
+        pb = PackedBatch(tables(method), nums, pos, dev)
+        st: dict = {}
+        res = run(pb, forces=True, state=st, tol=float(d["tol"]), maxiter=int(d["maxiter"]))
+        ms = []
+        for _ in range(max(1, min(steps, 3))):
+            s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            res = run(pb, forces=True, state=st, tol=float(d["tol"]), maxiter=int(d["maxiter"]))
+            e0.record()
+            e0.synchronize()
+            ms.append(s0.elapsed_time(e0))
+        e = res.energy.cpu().numpy()
+        g = res.gradient.cpu().numpy()
+        de = np.abs(e - d[f"{method}/energy"])
+        df = np.array([np.abs(g[pb.atom_off[i]: pb.atom_off[i + 1]] - d[f"{method}/gradient"][i, : nat[i]]).max()
+                       for i in range(pb.nmol)])
+        bad = (de > 1e-8) | (df > 1e-6)
+        out[f"config3_{method}"] = {
+            "workload": f"{method.upper()} E+F, 64 synthetic molecules of 30-120 atoms, packed batch",
+            "molecules_per_s": pb.nmol / (float(np.median(ms)) * 1e-3),
+            "ms_per_step": float(np.median(ms)),
+            "outside_tol": int(bad.sum()),
+            "outside_tol_not_chaotic": int(sum(1 for i in np.where(bad)[0] if i not in chaotic[method])),
+            "chaotic_excluded": sorted(chaotic[method]),
+            "max_abs_dE_others": float(max(de[i] for i in range(pb.nmol) if i not in chaotic[method])),
+            "max_abs_dF_others": float(max(df[i] for i in range(pb.nmol) if i not in chaotic[method])),
+        }
+    return out
+
+
 def main():
     a = args()
     world, rank, local = dist_setup()
@@ -435,6 +505,13 @@ def main():
                         "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,
                         "hbm_budget_gb": 120.0, "status_bad": sum(1 for r in out if r.status != 0)})
 
+    # the other single-GPU configurations: config 1 (one GFN1 molecule, E+F
+    # latency through the calculator) and config 3 (64 molecules of 30-120
+    # atoms, GFN1 and GFN2 E+F, packed, with parity on every molecule)
+    configs = None
+    if not a.no_configs and rank == 0:
+        configs = other_configs(dev, a.steps)
+
     # the serving configuration (8-300 atoms, both methods) through the two-lane loop
     config4 = None
     if a.config4:
@@ -521,6 +598,7 @@ def main():
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
         "serving": serving,
+        "configs": configs,
         "config4": config4,
         "gpu_launches": res.launches * a.steps,
         "clocks": clk,

@@ -296,14 +296,20 @@ class Calculator:
         chg = self._chrg_list(chrg, nmol)
         spins = None if spin is None else self._chrg_list(spin, nmol)
         key = (tuple(chg), None if spins is None else tuple(spins))
-        plist = [pos[i, : len(self._mols[i])] for i in range(nmol)]
         kw = dict(etemp=self.etemp, maxiter=self.maxiter, tol=self.tol, forces=forces,
                   gb=self.solvation, scf=self._scf)
         if self._pb is None or self._pb_key != key:
+            plist = [pos[i, : len(self._mols[i])] for i in range(nmol)]
             self._pb = engine.PackedBatch(self.tables, self._mols, plist, self.device, chg,
                                           [int(s) for s in spins] if spins else None)
             self._pb_key = key
             self._graphs = {}
+            # flat index of every real atom in the (nmol * nat_max) layout of
+            # the zero-padded input: one gather packs new positions, one
+            # scatter unpacks the gradient
+            nat_max = pos.shape[-2]
+            self._flat = torch.cat([i * nat_max + torch.arange(len(m)) for i, m in
+                                    enumerate(self._mols)]).to(self.device)
             from . import autotune
 
             autotune.ensure(self._pb)  # large batches: the tuned size-class policy
@@ -312,16 +318,17 @@ class Calculator:
             # the same molecules again (a geometry optimisation, MD, or a
             # repeated call): the second call captures the single point as a
             # CUDA graph, later calls replay it with the new positions
+            packed = pos.reshape(-1, 3)[self._flat]
             g = self._graphs.get(forces)
             if g is None:
-                self._pb.copy_positions_(plist)
+                self._pb.copy_positions_(packed)
                 g = engine.GraphStep(self._pb, **kw)
                 self._graphs[forces] = g
                 res = g.first
             else:
-                res = g.replay(plist)
+                res = g.replay(packed)
         else:
-            self._pb.copy_positions_(plist)
+            self._pb.copy_positions_(pos.reshape(-1, 3)[self._flat])
             res = engine.run(self._pb, state=self._state, **kw)
         st = res.status.cpu()
         bad = st[(st != 0)]
@@ -340,10 +347,8 @@ class Calculator:
             g = res.gradient
             if not self.include_rep:
                 raise NotImplementedError("gradient without repulsion")
-            grad = torch.zeros_like(pos)
-            off = self._pb.atom_off
-            for i in range(nmol):
-                grad[i, : len(self._mols[i])] = g[off[i] : off[i + 1]]
+            grad = torch.zeros_like(pos).reshape(-1, 3)
+            grad[self._flat] = g
             grad = grad.reshape(positions.shape)
         if not self.batched:
             energy = energy[0]

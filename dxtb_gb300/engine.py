@@ -147,9 +147,14 @@ class PackedBatch:
         self.positions = torch.cat([p.to(self.device) for p in pos]).contiguous()
         self._struct = None
 
-    def copy_positions_(self, positions: list) -> None:
+    def copy_positions_(self, positions) -> None:
         """Overwrite the device positions in place (same molecules), keeping
-        their address: a captured ``GraphStep`` reads them from there."""
+        their address: a captured ``GraphStep`` reads them from there.
+        ``positions``: a list of (nat_m, 3) arrays, or one packed (natoms, 3)
+        tensor."""
+        if torch.is_tensor(positions) and positions.shape == self.positions.shape:
+            self.positions.copy_(positions)
+            return
         pos = [torch.as_tensor(p, dtype=F64).reshape(-1, 3)[: int(self.nat[i])].to(self.device)
                for i, p in enumerate(positions)]
         self.positions.copy_(torch.cat(pos))
