@@ -101,10 +101,11 @@ class Server:
     requests would otherwise wait for the largest molecule admitted with
     them. Small requests may use an idle large slot while no large request
     is queued. ``large_sms`` caps the SMs that in-flight large packs hold
-    (``executor.team_sms(req)`` per molecule): the SCF kernels are persistent
-    and keep their SMs until the molecule converges, so without a cap the
-    large molecules' clusters can occupy every SM for seconds while small
-    requests wait. With ``order="size"`` each lane admits its smallest request
+    (``executor.team_sms(req)`` per molecule) while small requests are queued
+    or in flight: the SCF kernels are persistent and keep their SMs until the
+    molecule converges, so without a cap the large molecules' clusters can
+    occupy every SM for seconds while small requests wait; once no small
+    request is left, the large lane may use every SM. With ``order="size"`` each lane admits its smallest request
     first, and a pack takes only requests of at most twice its head's size
     (shortest job first: the percentiles of a burst of mixed sizes drop, the
     largest requests finish last). ``large_order`` overrides the order of
@@ -171,6 +172,12 @@ class Server:
             n = self.ex.norb(req) if hasattr(self.ex, "norb") else len(req.numbers)
             self._sizes[id(req)] = n
         return n
+
+    def _small_busy(self) -> bool:
+        """Small requests queued or in flight: the large lane's SM cap holds."""
+        return bool(self.queues["small"]) or any(
+            self._slot_lane(pk.slot) == "small" or self.lane(pk.requests[0]) == "small"
+            for pk in self.inflight)
 
     def _team_sms(self, req: Request) -> int:
         """SMs of a request's SCF team (cached), counted against ``large_sms``."""
@@ -247,7 +254,7 @@ class Server:
                                                 and self.free["large"]):
                     continue
                 head = q[0]
-                capped = lane == "large" and self.large_sms is not None
+                capped = lane == "large" and self.large_sms is not None and self._small_busy()
                 sms_free = (self.large_sms - self.sms_used) if capped else 0
                 if capped:
                     if self.sms_used == 0:

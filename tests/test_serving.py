@@ -183,22 +183,29 @@ def test_large_lane_sm_cap():
     ex.team_sms = lambda r: 16 if len(r.numbers) >= 250 else 8
     srv = Server(ex, hbm_budget=1e12, slots=6, max_pack=8, large_slots=5, large_n=200,
                  large_pack=1, order="size", large_order="longest", large_sms=24, clock=clk)
-    for rid, nat in enumerate([300, 280, 120, 150, 110]):
+    for rid, nat in enumerate([300, 280, 120, 150, 110, 20]):
         srv.submit(_req(rid, nat=nat))
     srv.pump()
-    # 300 (16 SMs) first; 280 (16) would exceed 24; 150 (8) fits; 120 waits
-    assert [ids for ids, _, _ in ex.launched] == [[0], [3]]
+    # the small request on the small slot; large: 300 (16 SMs) first, 280
+    # (16) would exceed 24 while a small request runs, 150 (8) fits, 120 waits
+    assert [ids for ids, slot, _ in ex.launched if slot == 0] == [[5]]
+    assert [ids for ids, slot, _ in ex.launched if slot > 0] == [[0], [3]]
     assert srv.sms_used == 24
-    while not srv.idle:
+    while srv._small_busy():
         srv.pump()
         assert srv.sms_used <= 24
+        clk.t += 0.001
+    # no small request left: the cap is lifted
+    while not srv.idle:
+        srv.pump()
         clk.t += 0.01
-    assert sorted(ids[0] for ids, _, _ in ex.launched) == [0, 1, 2, 3, 4]
+    assert sorted(ids[0] for ids, _, _ in ex.launched) == [0, 1, 2, 3, 4, 5]
     alone = Server(ex, hbm_budget=1e12, slots=2, max_pack=8, large_slots=1, large_n=200,
                    large_sms=8, clock=clk)
+    alone.submit(_req(8, nat=10))
     alone.submit(_req(9, nat=300))
     alone.pump()
-    assert ex.launched[-1][0] == [9] and alone.sms_used == 16
+    assert [9] in [ids for ids, _, _ in ex.launched] and alone.sms_used == 16
 
 
 def test_small_requests_borrow_idle_large_slots():
