@@ -519,12 +519,15 @@ def main():
                                         warm_up)
 
         reqs = poisson_requests(200, 2000.0, 4)
-        slots, large_slots = 8, 3
+        # 4 slots reserved for molecules under 160 orbitals, 8 for the rest
+        # (shortest first, packs of up to 32), whose SMs are capped at 112
+        # while small requests are queued or running
+        slots, large_slots = 12, 8
         ex = CudaExecutor(dev, slots=slots, priorities=[-100] * (slots - large_slots) + [0] * large_slots)
         warm_up(ex, slots)
         torch.cuda.synchronize()
         srv = Server(ex, hbm_budget=120e9, slots=slots, max_pack=32, large_slots=large_slots,
-                     large_n=320, large_pack=4, order="size")
+                     large_n=160, large_pack=32, order="size", large_sms=112)
         out = srv.serve(reqs)
         config4 = latency_summary(out)
         config4.update({
