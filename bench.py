@@ -528,8 +528,11 @@ def main():
         torch.cuda.synchronize()
         srv = Server(ex, hbm_budget=120e9, slots=slots, max_pack=32, large_slots=large_slots,
                      large_n=160, large_pack=32, order="size", large_sms=112)
+        c4_clocks = Clocks(local)
         out = srv.serve(reqs)
+        c4_clk = c4_clocks.stop()
         config4 = latency_summary(out)
+        config4["clocks"] = c4_clk
         config4.update({
             "workload": "200 requests, Poisson 2000/s (seed 4), GFN1/GFN2, 8-300 atoms log-uniform, E+F",
             "packs": srv.stats.packs, "max_inflight": srv.stats.max_inflight,

@@ -13,9 +13,12 @@ kernel then evaluates inf/inf = NaN. The Still kernel has the finite limit
 expressions).
 
     python -m dxtb_gb300.largesys [--maxiter K] [--count N]
+    python -m dxtb_gb300.largesys --atoms 310 --seed 9410 --method gfn1 --vacuum --maxiter 3
 
 Prints one JSON line with the wall time, the SCF time per iteration,
-iterations and residuals per molecule.
+iterations and residuals per molecule. With ``--atoms`` it runs one seeded
+random-walk molecule of that many atoms instead (the profiling case of a
+single large molecule on a 16-CTA cluster).
 """
 
 from __future__ import annotations
@@ -37,24 +40,37 @@ def main(argv=None) -> None:
     p.add_argument("--maxiter", type=int, default=250)
     p.add_argument("--count", type=int, default=8)
     p.add_argument("--kernel", default="still", choices=["still", "p16"])
+    p.add_argument("--atoms", type=int, default=0, help="one molecule of this many atoms")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--method", default="gfn2", choices=["gfn1", "gfn2"])
+    p.add_argument("--vacuum", action="store_true", help="no solvation")
+    p.add_argument("--no-forces", action="store_true")
     a = p.parse_args(argv)
     t0 = time.time()
-    mols = config_molecules(5, count=a.count)
+    if a.atoms > 0:
+        from .workloads import random_molecule
+
+        mols = [random_molecule(a.seed, a.atoms)]
+    else:
+        mols = config_molecules(5, count=a.count)
     t_gen = time.time() - t0
-    gb = {"epsilon": 78.4, "alpb": False, "kernel": a.kernel}
-    pb = PackedBatch(tables("gfn2"), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols])
+    gb = None if a.vacuum else {"epsilon": 78.4, "alpb": False, "kernel": a.kernel}
+    pb = PackedBatch(tables(a.method), [m[0] for m in mols], [torch.tensor(m[1]) for m in mols])
     torch.cuda.synchronize()
     ev: dict = {}
     t = time.time()
-    res = run(pb, forces=True, gb=gb, maxiter=a.maxiter, events=ev)
+    res = run(pb, forces=not a.no_forces, gb=gb, maxiter=a.maxiter, events=ev)
     torch.cuda.synchronize()
     wall = time.time() - t
     e4 = res.state["energies"][: 4 * pb.nmol].view(-1, 4).cpu().numpy()
     its = e4[:, 2]
     stages = {k: v[0].elapsed_time(v[1]) / 1e3 for k, v in ev.items()}
-    g = res.gradient.cpu().numpy()
+    g = res.gradient.cpu().numpy() if res.gradient is not None else np.zeros(1)
     out = {
-        "workload": "GFN2 + GB (Still, eps 78.4) E+F, synthetic 1000-2000-atom molecules",
+        "workload": (f"{a.method.upper()} {'vacuum' if gb is None else 'GB'} "
+                     f"{'E' if a.no_forces else 'E+F'}, one molecule of {a.atoms} atoms (seed {a.seed})"
+                     if a.atoms > 0 else
+                     "GFN2 + GB (Still, eps 78.4) E+F, synthetic 1000-2000-atom molecules"),
         "molecules": pb.nmol,
         "atoms": [int(v) for v in pb.nat],
         "nao": [int(v) for v in pb.nao],
