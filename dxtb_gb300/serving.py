@@ -24,7 +24,9 @@ batched single point of ``engine.run``.
 from __future__ import annotations
 
 import math
+import os
 import time
+import warnings
 from collections import deque
 from dataclasses import dataclass, field
 
@@ -397,6 +399,18 @@ class CudaExecutor:
         from . import _lib
         from .params import Tables
 
+        # every slot stream forks up to six class streams in the library:
+        # with the driver's default of 8 hardware queues, streams share
+        # queues and a small pack's kernels can wait behind a long-running
+        # large one on the same queue (measured on the serving stream: p50
+        # 9.9 s with 8 queues, 3.9 s with 32). The variable only takes
+        # effect before the CUDA context exists.
+        if not torch.cuda.is_initialized():
+            os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+        elif int(os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")) < 32:
+            warnings.warn("CUDA was initialised with fewer than 32 hardware queues "
+                          "(CUDA_DEVICE_MAX_CONNECTIONS): concurrent packs may serialise",
+                          stacklevel=2)
         _lib.lib()  # fails loudly without the CUDA library
         self.torch = torch
         self.device = torch.device(device)
