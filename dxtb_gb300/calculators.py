@@ -320,11 +320,21 @@ class Calculator:
             # CUDA graph, later calls replay it with the new positions
             packed = pos.reshape(-1, 3)[self._flat]
             g = self._graphs.get(forces)
-            if g is None:
+            if g is None and forces not in self._graphs:
                 self._pb.copy_positions_(packed)
-                g = engine.GraphStep(self._pb, **kw)
+                try:
+                    g = engine.GraphStep(self._pb, **kw)
+                    res = g.first
+                except RuntimeError as err:
+                    # a capture the driver refuses: keep the eager launches
+                    warnings.warn(f"CUDA graph capture failed ({err}); launching eagerly",
+                                  stacklevel=3)
+                    g = None
+                    res = engine.run(self._pb, state=self._state, **kw)
                 self._graphs[forces] = g
-                res = g.first
+            elif g is None:
+                self._pb.copy_positions_(packed)
+                res = engine.run(self._pb, state=self._state, **kw)
             else:
                 res = g.replay(packed)
         else:

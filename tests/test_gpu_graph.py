@@ -97,3 +97,4 @@ def test_calculator_repeated_calls_replay_the_graph():
         assert (e - e_ref).abs().max().item() <= ATOL
         assert (f - f_ref).abs().max().item() <= ATOL
     assert set(graph_calc._graphs) == {False, True}
+    assert all(g is not None for g in graph_calc._graphs.values())  # captured, not eager
