@@ -396,22 +396,30 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nty = (int)(blockDim.x >> 5);
   const int C = tm.size, rk = tm.rank;
   const int nown = (n + C - 1) / C;  // the same bound on every CTA
-  double *R, *sc0 = nullptr;
-  size_t ldr;
-  if (srows != nullptr && (int64_t)(nown + (CL ? 1 : 0)) * n <= rows_cap) {
-    R = srows;
-    ldr = (size_t)n;
-    if (CL) sc0 = srows + (size_t)nown * n;
-    for (int64_t t = threadIdx.x; t < (int64_t)nown * n; t += blockDim.x) {
-      const int j = (int)(t / n), c = (int)(t % n), i = rk + C * j;
-      if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
+  // Own row i = rk + C j lives in shared memory for j >= jsm (the rows that
+  // stay in the trailing matrix longest) and in place in A below that. All
+  // of them fit up to n ~ 450 at C = 8; above, as many as the shared memory
+  // holds beside the broadcast row (a third of them at n ~ 1000, C = 16).
+  // nsm and the layout are the same on every CTA of a cluster.
+  int jsm = nown;
+  double *sc0 = nullptr;
+  if (srows != nullptr && rows_cap > 0) {
+    const int64_t fit = rows_cap / n - (CL ? 1 : 0);  // whole rows beside the broadcast row
+    if (fit >= 1) {
+      const int nsm = (int)(fit < (int64_t)nown ? fit : (int64_t)nown);
+      jsm = nown - nsm;
+      if (CL) sc0 = srows + (size_t)nsm * n;
+      for (int64_t t = threadIdx.x; t < (int64_t)nsm * n; t += blockDim.x) {
+        const int j = jsm + (int)(t / n), c = (int)(t % n), i = rk + C * j;
+        if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-  } else {
-    R = A + (size_t)rk * n;
-    ldr = (size_t)C * n;
   }
-  auto rowp = [&](int i) -> double * { return R + (size_t)((i - rk) / C) * ldr; };  // own global row i
+  auto rowp = [&](int i) -> double * {  // own global row i
+    const int j = (i - rk) / C;
+    return j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)i * n;
+  };
   // scalars of step k from su[0..m): warp 0 (the lead's lane 0 stores tau, e)
   auto scalars = [&](int k, int m) {
     double p0 = 0.0, p1 = 0.0;
@@ -562,7 +570,7 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
         d[n - 1] = rowp(n - 1)[n - 1];
       }
     } else if (rk == 0) {
-      d[0] = R[0];
+      d[0] = rowp(0)[0];
     }
     if (tm.lead()) {
       if (n >= 2) tau[n - 2] = 0.0;

@@ -1029,13 +1029,13 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     return DXTB_ERR_LAUNCH;
   // shared memory of class c: the base plus the rows of the Householder
   // reduction of its largest possible molecule (and, for clusters, one
-  // broadcast row), when they fit
+  // broadcast row), or as many of them as the CTA's shared memory holds
   auto class_smem = [&](int c) -> size_t {
     const int csize = c >= 2 ? 1 << (c - 1) : 1;
     const int nub = (c + 1 < kClasses && a.thr[c + 1] != INT32_MAX) ? min(nmax, a.thr[c + 1] - 1) : nmax;
     const int rows = (nub + csize - 1) / csize + (c >= 2 ? 1 : 0);
     const size_t full = smem + (size_t)rows * nub * sizeof(double);
-    return full <= (size_t)kMaxDynSmem ? full : smem;
+    return full <= (size_t)kMaxDynSmem ? full : (size_t)kMaxDynSmem;
   };
   // largest classes first: clusters, then one-SM CTAs, then the shared SMs
   for (int c = cmax; c >= 2; --c) {
