@@ -451,7 +451,12 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
     const int m = n - k - 1;
     const int rb = ((rk - (k + 1)) % C + C) % C;          // first own local row
     const int mc = rb < m ? (m - rb + C - 1) / C : 0;      // own local rows rb + C jj
-    auto lrow = [&](int jj) -> double * { return rowp(k + 1 + rb + C * jj) + (k + 1); };
+    // own row k + 1 + rb + C jj is local row j0 + jj (k + 1 + rb - rk is a multiple of C)
+    const int j0 = (k + 1 + rb - rk) / C;
+    auto lrow = [&](int jj) -> double * {
+      const int j = j0 + jj;
+      return (j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)(rk + C * j) * n) + (k + 1);
+    };
     if (threadIdx.x == 0 && k % C == rk) d[k] = rowp(k)[k];
     const double t = sscal[0], scale = sscal[1];
     // ---- A ----

@@ -1029,13 +1029,19 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
     return DXTB_ERR_LAUNCH;
   // shared memory of class c: the base plus the rows of the Householder
   // reduction of its largest possible molecule (and, for clusters, one
-  // broadcast row), or as many of them as the CTA's shared memory holds
+  // broadcast row). When they do not all fit, the CTA takes the most shared
+  // memory if that still holds 60 % of the rows; below that the rows stay in
+  // L1/L2 (shared memory is carved out of L1, and a large carve-out holding a
+  // third of the rows measured 2-5 % slower than none at n ~ 900-1000)
   auto class_smem = [&](int c) -> size_t {
     const int csize = c >= 2 ? 1 << (c - 1) : 1;
     const int nub = (c + 1 < kClasses && a.thr[c + 1] != INT32_MAX) ? min(nmax, a.thr[c + 1] - 1) : nmax;
-    const int rows = (nub + csize - 1) / csize + (c >= 2 ? 1 : 0);
+    const int nown = (nub + csize - 1) / csize;
+    const int rows = nown + (c >= 2 ? 1 : 0);
     const size_t full = smem + (size_t)rows * nub * sizeof(double);
-    return full <= (size_t)kMaxDynSmem ? full : (size_t)kMaxDynSmem;
+    if (full <= (size_t)kMaxDynSmem) return full;
+    const int64_t fit = ((int64_t)kMaxDynSmem / 8 - 4 * (int64_t)nub) / nub - (c >= 2 ? 1 : 0);
+    return 10 * fit >= 6 * (int64_t)nown ? (size_t)kMaxDynSmem : smem;
   };
   // largest classes first: clusters, then one-SM CTAs, then the shared SMs
   for (int c = cmax; c >= 2; --c) {
