@@ -401,24 +401,42 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
   // of them fit up to n ~ 450 at C = 8; above, as many as the shared memory
   // holds beside the broadcast row (a third of them at n ~ 1000, C = 16).
   // nsm and the layout are the same on every CTA of a cluster.
+  // A one-CTA team (n < 136 here) keeps all its rows in shared memory or
+  // none of them.
   int jsm = nown;
   double *sc0 = nullptr;
+  double *R = A + (size_t)rk * n;
+  size_t ldr = (size_t)C * n;
   if (srows != nullptr && rows_cap > 0) {
-    const int64_t fit = rows_cap / n - (CL ? 1 : 0);  // whole rows beside the broadcast row
-    if (fit >= 1) {
-      const int nsm = (int)(fit < (int64_t)nown ? fit : (int64_t)nown);
-      jsm = nown - nsm;
-      if (CL) sc0 = srows + (size_t)nsm * n;
-      for (int64_t t = threadIdx.x; t < (int64_t)nsm * n; t += blockDim.x) {
-        const int j = jsm + (int)(t / n), c = (int)(t % n), i = rk + C * j;
+    if constexpr (CL) {
+      const int64_t fit = rows_cap / n - 1;  // whole rows beside the broadcast row
+      if (fit >= 1) {
+        const int nsm = (int)(fit < (int64_t)nown ? fit : (int64_t)nown);
+        jsm = nown - nsm;
+        sc0 = srows + (size_t)nsm * n;
+        for (int64_t t = threadIdx.x; t < (int64_t)nsm * n; t += blockDim.x) {
+          const int j = jsm + (int)(t / n), c = (int)(t % n), i = rk + C * j;
+          if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
+        }
+        __syncthreads();
+      }
+    } else if ((int64_t)nown * n <= rows_cap) {
+      R = srows;
+      ldr = (size_t)n;
+      for (int64_t t = threadIdx.x; t < (int64_t)nown * n; t += blockDim.x) {
+        const int j = (int)(t / n), c = (int)(t % n), i = rk + C * j;
         if (i < n) srows[t] = ld<CL>(A + (size_t)i * n + c);
       }
       __syncthreads();
     }
   }
   auto rowp = [&](int i) -> double * {  // own global row i
-    const int j = (i - rk) / C;
-    return j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)i * n;
+    if constexpr (CL) {
+      const int j = (i - rk) / C;
+      return j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)i * n;
+    } else {
+      return R + (size_t)((i - rk) / C) * ldr;
+    }
   };
   // scalars of step k from su[0..m): warp 0 (the lead's lane 0 stores tau, e)
   auto scalars = [&](int k, int m) {
@@ -454,8 +472,12 @@ __device__ void team_tridiag(Team<CL> &tm, int n, double *A, double *d, double *
     // own row k + 1 + rb + C jj is local row j0 + jj (k + 1 + rb - rk is a multiple of C)
     const int j0 = (k + 1 + rb - rk) / C;
     auto lrow = [&](int jj) -> double * {
-      const int j = j0 + jj;
-      return (j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)(rk + C * j) * n) + (k + 1);
+      if constexpr (CL) {
+        const int j = j0 + jj;
+        return (j >= jsm ? srows + (size_t)(j - jsm) * n : A + (size_t)(rk + C * j) * n) + (k + 1);
+      } else {
+        return rowp(k + 1 + rb + C * jj) + (k + 1);
+      }
     };
     if (threadIdx.x == 0 && k % C == rk) d[k] = rowp(k)[k];
     const double t = sscal[0], scale = sscal[1];
