@@ -1031,8 +1031,8 @@ static int32_t launch_scf(ScfArgs a, int nmol, cudaStream_t st, const GradArgs *
   // reduction of its largest possible molecule (and, for clusters, one
   // broadcast row). When they do not all fit, the CTA takes the most shared
   // memory if that still holds 60 % of the rows; below that the rows stay in
-  // L1/L2 (shared memory is carved out of L1, and a large carve-out holding a
-  // third of the rows measured 2-5 % slower than none at n ~ 900-1000)
+  // L1/L2 (shared memory is carved out of L1; a carve-out holding a fifth to
+  // a third of the rows gained nothing at n ~ 900-1000)
   auto class_smem = [&](int c) -> size_t {
     const int csize = c >= 2 ? 1 << (c - 1) : 1;
     const int nub = (c + 1 < kClasses && a.thr[c + 1] != INT32_MAX) ? min(nmax, a.thr[c + 1] - 1) : nmax;
