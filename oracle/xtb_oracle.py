@@ -1051,6 +1051,46 @@ def gradient(sysm: System, positions, p, w, n0, solvation=None, exclude=()) -> t
     return g
 
 
+HALOGENS = (17, 35, 53, 85)   # components/classicals/halogen/hal.py: donors
+XB_BASES = (7, 8, 15, 16)     # and acceptors
+XB_CUTOFF = 20.0              # constants/xtb.py DEFAULT_XB_CUTOFF
+
+
+def halogen_energy(par: dict, numbers, positions) -> torch.Tensor:
+    """
+    GFN1 halogen-bond correction (``components/classicals/halogen/hal.py``,
+    ``_xbond_list`` and ``_xbond_energy``): for every donor X and acceptor J
+    within the cutoff, with K the nearest other atom of X,
+    E_X += xbond_X (l12 - damp l6) / (1 + l12) (1/2 - cos(J-X-K) / 4)^6,
+    l6 = ((R_X + R_J) rscale / r_XJ)^6 with the atomic radii of the H0
+    distance polynomial. Differentiable in ``positions``.
+    """
+    z = [int(v) for v in np.asarray(numbers).ravel()]
+    pos = torch.as_tensor(positions, dtype=DT)
+    xb = par["halogen"]["classical"]
+    damp, rscale = float(xb["damping"]), float(xb["rscale"])
+    e = torch.zeros((), dtype=DT)
+    for x, zx in enumerate(z):
+        if zx not in HALOGENS:
+            continue
+        strength = float(par["element"][zx].get("xbond", 0.0))
+        d = ((pos - pos[x]) ** 2).sum(-1)
+        dk = d.detach().clone()
+        dk[x] = float("inf")
+        k = int(torch.argmin(dk))
+        for j, zj in enumerate(z):
+            if zj not in XB_BASES or float(dk[j].sqrt()) > XB_CUTOFF:
+                continue
+            r0 = (_radii.ATOMIC_RADII[zx] + _radii.ATOMIC_RADII[zj]) * rscale
+            l6 = (r0**2 / d[j]) ** 3
+            l12 = l6 * l6
+            lj = (l12 - damp * l6) / (1.0 + l12)
+            dkj = ((pos[k] - pos[j]) ** 2).sum()
+            cosa = (d[k] + d[j] - dkj) / torch.sqrt(d[k] * d[j])
+            e = e + strength * lj * (0.5 - 0.25 * cosa) ** 6
+    return e
+
+
 def dipole_moment(sysm: System, positions, p) -> torch.Tensor:
     """
     Electric dipole moment (e a0) at the density ``p``: the valence charges

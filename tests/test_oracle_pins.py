@@ -212,3 +212,33 @@ def test_gfn1_scf_energies(name):
     chrg = float(G[f"scf/{name}/charge"]) if f"scf/{name}/charge" in G.files else 0.0
     r = X.singlepoint("gfn1", num, pos, chrg=chrg, tol=1e-10, maxiter=250, exclude=("rep",))
     assert abs(r.energy - float(G[f"scf/{name}/egfn1"])) < np.sqrt(np.finfo(np.float64).eps) * 10
+
+
+def test_gfn1_halogen_term_is_zero_for_accepted_elements(monkeypatch):
+    """The GFN1 halogen-bond correction (components/classicals/halogen/
+    hal.py): its bond strengths are nonzero only for Br, I and At, so for
+    every element up to Ar the term vanishes, as in the reference's fixture
+    for MB16_43_01 (test/test_classical/test_halogen/samples.py: energy and
+    gradient zero), whose Cl has N and O acceptors within the cutoff. With a
+    planted strength on Cl the restated term is nonzero and its autograd
+    gradient matches central differences."""
+    par = X.load_par("gfn1")
+    strengths = {z: float(par["element"][z].get("xbond", 0.0)) for z in par["element"]}
+    assert all(strengths[z] == 0.0 for z in range(1, 19))
+    assert all(strengths[z] > 0.0 for z in (35, 53, 85))
+    num, pos = mol("MB16_43_01")
+    assert 17 in num.tolist() and {7, 8} & set(num.tolist())
+    assert float(X.halogen_energy(par, num, pos)) == 0.0
+    monkeypatch.setitem(par["element"][17], "xbond", 0.02)
+    p = torch.tensor(pos, requires_grad=True)
+    e = X.halogen_energy(par, num, p)
+    assert abs(float(e.detach())) > 1e-6
+    (g,) = torch.autograd.grad(e, p)
+    h = 1e-5
+    for a, x in [(int(np.where(num == 17)[0][0]), 0), (int(np.where(num == 8)[0][0]), 2)]:
+        q = pos.copy()
+        q[a, x] += h
+        ep = float(X.halogen_energy(par, num, q))
+        q[a, x] -= 2 * h
+        em = float(X.halogen_energy(par, num, q))
+        assert abs((ep - em) / (2 * h) - float(g[a, x])) < 1e-8
