@@ -113,3 +113,23 @@ def test_projection_removes_rigid_motions():
         vib = vib_analysis(z, pos, hess)
         scale = torch.linalg.matrix_norm(rig.T @ rig, ord=2).item()
         assert (vib.freqs**2).max().item() < 1e-14 * scale
+
+
+def test_linear_molecules_keep_3n_minus_5_modes():
+    """A linear triatomic (collinear, off the coordinate axes) projects five
+    rigid motions and keeps 3 nat - 5 = 4 modes; bending it gives 3."""
+    from dxtb_gb300.properties import is_linear, vib_analysis
+
+    axis = torch.tensor([1.0, 2.0, -0.5], dtype=torch.float64)
+    axis = axis / axis.norm()
+    lin = torch.stack([0.0 * axis, 2.2 * axis, 4.4 * axis]) + torch.tensor([0.3, -1.0, 2.0])
+    assert is_linear(lin)
+    bent = lin.clone()
+    bent[2] += torch.tensor([0.0, 0.3, 0.0], dtype=torch.float64)
+    assert not is_linear(bent)
+    z = [8, 6, 8]
+    for pos, nmodes in ((lin, 4), (bent, 3)):
+        h = torch.eye(9, dtype=torch.float64).view(3, 3, 3, 3) * 0.5
+        vib = vib_analysis(z, pos, h)
+        assert vib.modes.shape == (9, nmodes)
+        assert (vib.freqs > 0).all()
